@@ -1,0 +1,303 @@
+"""Benchmark: circuit time of the 14-qubit mixed-gate workload (FP64 rho, 4^14
+entries = 4.3 GB, 2000 gates drawn uniformly from the 29-entry table on random
+distinct qubits), fused passes vs the plain gate-by-gate path, on one GB300.
+
+One step = one run of the whole circuit on the device-resident rho (a CUDA
+graph replay of every pass).  ``value`` is seconds per circuit of the fused
+path (lower is better), device-timed with CUDA events on the engine's stream.
+Extra keys: the plain path's time and the speed-up, the fused-vs-plain error
+(the plain path judges every fused result), the roofline of the dominant pass
+kernel, ``e2e`` through the C ABI with host buffers (the circuit and rho cross
+the host boundary every step), and a CPU baseline of the reference's CPU
+algorithm (the oracle port, all host cores) on a bounded prefix sample.
+
+    python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl reference]
+                    [--n 14] [--gates 2000] [--planner greedy|learned] [--max-k 4]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [os.path.join(ROOT, "dm-sim_gb300", "python"), ROOT]
+
+import numpy as np  # noqa: E402
+
+import dmsim_workloads as W  # noqa: E402
+
+CLASS_NAMES = ["MOVE", "SIGNED", "PHASE", "DENSE", "SPARSE", "RLIN"]
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9 or f[0] != "0":
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload(n, gates):
+    return W.table_mix(n, gates, seed=2)
+
+
+def cpu_sample(n, circ, budget_s, threads):
+    """Time the reference's CPU algorithm (oracle port) on a prefix of the
+    circuit at full size and extrapolate per basic gate.  Returns seconds per
+    circuit and a description of the sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    total_basic = sum(O.basic_count(g) for g in circ)
+    # grow the prefix until the sample takes ~budget_s
+    k = 1
+    t = 0.0
+    nb = 0
+    while True:
+        pre = circ[:k]
+        nb = sum(O.basic_count(g) for g in pre)
+        t0 = time.perf_counter()
+        O.dm_sim(n, pre, nthreads=threads)
+        t = time.perf_counter() - t0
+        if t >= budget_s / 3 or k >= len(circ):
+            break
+        k = min(len(circ), max(k + 1, int(k * max(2.0, budget_s / 3 / max(t, 1e-3)))))
+    per_basic = t / max(nb, 1)
+    return per_basic * total_basic, f"first {k} of {len(circ)} gates ({nb} of {total_basic} basic gates) at n={n}, " \
+                                    f"{t:.1f} s, extrapolated per basic gate"
+
+
+def run_reference_arm(args, n, circ):
+    threads = os.cpu_count() or 1
+    value, sample = cpu_sample(n, circ, args.cpu_budget, threads)
+    vals = [value]
+    for _ in range(max(0, args.steps - 1)):
+        v, _ = cpu_sample(n, circ, args.cpu_budget, threads)
+        vals.append(v)
+    v = float(np.mean(vals))
+    line = {"impl": "reference", "metric": f"{n}q mixed-gate circuit time (reference CPU algorithm)", "value": v,
+            "unit": "s/circuit", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"table_mix n={n} gates={len(circ)} seed=2", "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": v, "unit": "s/circuit", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "s/circuit", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine")
+    ap.add_argument("--n", type=int, default=14)
+    ap.add_argument("--gates", type=int, default=2000)
+    ap.add_argument("--planner", default="greedy")
+    ap.add_argument("--max-k", type=int, default=4)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    n = args.n
+    circ = workload(n, args.gates)
+
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference_arm(args, n, circ)
+        return
+
+    import dmsim_gb300 as E  # fails loudly if the engine library is missing
+
+    if world > 1:
+        # replicas only: every rank runs the same single-GPU workload on its own device
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    hbm_peak, peak_kind = peaks()
+
+    # ---- fused path: the timed steps
+    fused = E.Simulation(n, mode="fused", max_k=args.max_k, planner=args.planner)
+    t_up0 = time.perf_counter()
+    fused.extend(circ)
+    fused.upload()
+    upload_s = time.perf_counter() - t_up0
+    npasses, nbasic = fused.plan_stats()
+    for _ in range(args.warmup):
+        fused.run()
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    ms = []
+    for _ in range(args.steps):
+        fused.run()
+        ms.append(fused.last_timings()["ms"])
+    wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    step_ms = float(np.mean(ms))
+    if world > 1:
+        import torch
+        t = torch.tensor([step_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+    bytes_per_run = fused.last_timings()["bytes"]
+
+    # ---- per-pass profile of one fused run (untimed): the dominant kernel
+    fused.set_option(E.OPT_RECORD, 1)
+    fused.run()
+    rec = fused.pass_records()
+    fused.set_option(E.OPT_RECORD, 0)
+    groups = {}
+    for r in rec:
+        key = (int(r[0]), int(r[1]))
+        g = groups.setdefault(key, [0, 0.0, 0.0])
+        g[0] += 1
+        g[1] += r[6]
+        g[2] += r[7]
+    tot_ms = sum(g[1] for g in groups.values())
+    dom = max(groups.items(), key=lambda kv: kv[1][1])
+    (dK, dcls), (dcount, dms, dbytes) = dom
+    dom_name = f"k_pass<double,{dK},{CLASS_NAMES[dcls]}>"
+    achieved = dbytes / (dms * 1e-3) / 1e9
+    kernels = {f"K{k}_{CLASS_NAMES[c]}": {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot_ms, 4),
+                                          "GBps": round(v[2] / (v[1] * 1e-3) / 1e9, 1)}
+               for (k, c), v in sorted(groups.items(), key=lambda kv: -kv[1][1])}
+
+    # ---- plain path (the reference's method) and the fused-vs-plain error
+    plain_s = None
+    err = None
+    plain_bytes = None
+    plain_passes = None
+    if not args.no_plain:
+        plain = E.Simulation(n, mode="plain")
+        plain.extend(circ)
+        plain.upload()
+        plain.run()
+        plain_s = plain.last_timings()["ms"] / 1e3
+        plain_bytes = plain.last_timings()["bytes"]
+        plain_passes = plain.plan_stats()[0]
+        fused.reset_dm()
+        fused.run()
+        err = fused.compare(plain)
+        plain.close()
+
+    # ---- end to end through the C ABI with host buffers
+    N = 1 << (2 * n)
+    pre = E.PinnedBuffer(N)
+    pim = E.PinnedBuffer(N)
+    e2e = []
+    desc_bytes = 0
+    for _ in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        fused.reset()                 # clear the circuit, rho = |0..0><0..0|
+        fused.extend(circ)            # the circuit crosses the host boundary
+        fused.upload()                # descriptors H2D
+        fused.run()
+        fused.get_dm_into(pre.array, pim.array)  # rho D2H (the reference's sim() copies it back)
+        e2e.append(time.perf_counter() - t0)
+    pre.close()
+    pim.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, sample = cpu_sample(n, circ, args.cpu_budget, threads)
+        cpu = {"value": v, "unit": "s/circuit", "cores": threads, "kind": "port", "sample": sample}
+
+    if rank == 0:
+        value = step_ms / 1e3
+        line = {
+            "metric": f"{n}q mixed-gate circuit time, fused FP64 passes (plain gate-by-gate path beside it)",
+            "value": value, "unit": "s/circuit", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded circuits, state from |0..0><0..0|)",
+            "config": {"workload": f"table_mix n={n} gates={len(circ)} seed=2 (29-entry table, random distinct qubits)",
+                       "planner": args.planner, "max_k": args.max_k, "passes": npasses, "basic_gates": nbasic,
+                       "l2": "inputs larger than L2 (rho = %.1f GB)" % (16.0 * N / 1e9), "parallelism": "replicas"},
+            "plain_s": plain_s, "plain_passes": plain_passes,
+            "speedup_fused_vs_plain": (plain_s / value) if plain_s else None,
+            "fused_vs_plain_error": err,
+            "hbm_GBps_fused_run": bytes_per_run / (step_ms * 1e-3) / 1e9,
+            "hbm_GBps_plain_run": (plain_bytes / plain_s / 1e9) if plain_s else None,
+            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": hbm_peak,
+                         "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": None,
+                         "peak_kind": peak_kind, "launches": dcount},
+            "kernels": kernels,
+            "e2e": {"value": float(np.mean(e2e)), "unit": "s/circuit",
+                    "h2d_bytes_per_step": int(npasses * 4096), "d2h_bytes_per_step": int(16 * N)},
+            "gpu_launches": int(npasses * args.steps),
+            "clocks": clk,
+            "upload_s": upload_s,
+            "wall_s_timed": wall,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    fused.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

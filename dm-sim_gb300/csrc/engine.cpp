@@ -1,0 +1,734 @@
+// engine.cpp -- the Simulation object behind the C ABI (include/dmsim_gb300.h).
+//
+// Life cycle as DM-Sim's Simulation (src/dmsim_nvgpu_omp.cuh:193-814):
+// append() collects gates, upload() decomposes them into basic gates, plans
+// the passes (one per basic gate in plain mode, fused k<=4 operators in fused
+// mode), writes all pass descriptors to the device in one copy and captures
+// the launch sequence in a CUDA graph; run() replays it.  rho stays resident
+// in HBM across runs (chained circuits), in the reference's result layout.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/dmsim_gb300.h"
+#include "engine_internal.h"
+#include "gates.h"
+#include "kernels.h"
+#include "metrics.h"
+#include "plan.h"
+
+using namespace dmg;
+
+namespace {
+
+struct DmError {
+  int code;
+  std::string msg;
+};
+
+#define DM_CUDA(call)                                                                         \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      throw DmError{e_ == cudaErrorMemoryAllocation ? DMSIM_ERR_OOM : DMSIM_ERR_CUDA,         \
+                    std::string(#call) + ": " + cudaGetErrorString(e_)};                      \
+  } while (0)
+
+}  // namespace
+
+struct dmsim_sim {
+  uint32_t n = 0;
+  uint64_t dim = 0, N = 0;
+  int device = 0, sms = 0;
+  bool fp32 = false;
+  void* d_re = nullptr;
+  void* d_im = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double* d_diag = nullptr;
+  double* d_acc = nullptr;
+
+  std::vector<GateRec> circuit;
+  bool uploaded = false;
+  std::vector<PassInfo> passes;
+  void* d_desc = nullptr;
+  size_t desc_bytes = 0;
+  uint32_t n_basic = 0;
+  cudaGraphExec_t gexec = nullptr;
+
+  int mode = 0, maxk = 4, planner = 0, record = 0, graph_on = 1, verbose = 0;
+  int64_t seed = -1;
+
+  double last_ms = 0, last_bytes = 0;
+  std::vector<PassRecord> records;
+  std::string err;
+};
+
+namespace {
+
+size_t esize(const dmsim_sim* s) { return s->fp32 ? 4 : 8; }
+
+void free_plan(dmsim_sim* s) {
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  s->gexec = nullptr;
+  if (s->d_desc) cudaFree(s->d_desc);
+  s->d_desc = nullptr;
+  s->desc_bytes = 0;
+  s->passes.clear();
+  s->n_basic = 0;
+  s->uploaded = false;
+}
+
+void free_state(dmsim_sim* s) {
+  if (s->d_re) cudaFree(s->d_re);
+  if (s->d_im) cudaFree(s->d_im);
+  s->d_re = s->d_im = nullptr;
+}
+
+void ensure_state(dmsim_sim* s) {
+  if (s->d_re) return;
+  const size_t bytes = s->N * esize(s);
+  DM_CUDA(cudaSetDevice(s->device));
+  if (cudaMalloc(&s->d_re, bytes) != cudaSuccess) {
+    s->d_re = nullptr;
+    cudaGetLastError();
+    throw DmError{DMSIM_ERR_OOM, "device allocation of rho (real part) failed"};
+  }
+  if (cudaMalloc(&s->d_im, bytes) != cudaSuccess) {
+    cudaFree(s->d_re);
+    s->d_re = nullptr;
+    s->d_im = nullptr;
+    cudaGetLastError();
+    throw DmError{DMSIM_ERR_OOM, "device allocation of rho (imaginary part) failed"};
+  }
+  DM_CUDA(launch_set_zero_state(s->d_re, s->d_im, s->N, s->fp32, s->stream));
+  DM_CUDA(cudaStreamSynchronize(s->stream));
+}
+
+void check_qubits(const dmsim_sim* s, const GateRec& g) {
+  const int ar = gate_arity(g.op);
+  if (ar == 0) throw DmError{DMSIM_ERR_ARG, "unknown gate id " + std::to_string(g.op)};
+  // the reference asserts every qubit slot < n_qubits (:334-338)
+  for (int i = 0; i < 5; i++)
+    if (g.qb[i] >= s->n) throw DmError{DMSIM_ERR_ARG, "qubit index out of range"};
+  for (int i = 0; i < ar; i++)
+    for (int j = i + 1; j < ar; j++)
+      if (g.qb[i] == g.qb[j]) throw DmError{DMSIM_ERR_ARG, "a gate's qubits must be distinct"};
+}
+
+// Launch the planned passes on the stream (captured or direct).
+void enqueue_passes(dmsim_sim* s, bool timed) {
+  for (size_t i = 0; i < s->passes.size(); i++) {
+    PassInfo& p = s->passes[i];
+    LaunchArgs a;
+    a.re = s->d_re;
+    a.im = s->d_im;
+    a.desc = static_cast<const char*>(s->d_desc) + p.desc_off;
+    a.K = p.K;
+    a.cls = p.cls;
+    a.fp32 = s->fp32;
+    a.grid = p.grid;
+    a.tile_entries = p.tile_entries;
+    if (timed) DM_CUDA(cudaEventRecord(p.ev0, s->stream));
+    DM_CUDA(launch_pass(a, s->stream));
+    if (timed) DM_CUDA(cudaEventRecord(p.ev1, s->stream));
+  }
+}
+
+void upload(dmsim_sim* s) {
+  if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "upload() called twice without clear_circuit() (:347-350)"};
+  ensure_state(s);
+  std::vector<Basic> basics;
+  for (const GateRec& g : s->circuit) decompose(g, basics);
+  s->n_basic = (uint32_t)basics.size();
+  std::vector<PassSpec> specs;
+  if (s->mode == 0) specs = plan_plain(basics);
+  else if (s->planner == 1) throw DmError{DMSIM_ERR_UNSUPPORTED, "the learned planner is not available in this build"};
+  else specs = plan_greedy(basics, s->maxk);
+  // descriptors, 256-byte aligned, one host blob, one copy
+  std::vector<size_t> offs;
+  size_t total = 0;
+  for (const PassSpec& p : specs) {
+    offs.push_back(total);
+    total += (desc_size(p.K) + 255) & ~(size_t)255;
+  }
+  std::vector<unsigned char> blob(std::max<size_t>(total, 256));
+  s->passes.clear();
+  for (size_t i = 0; i < specs.size(); i++) {
+    PassInfo pi;
+    std::memset(&pi, 0, sizeof pi);
+    uint64_t ntiles = 0;
+    int tile = 0;
+    const uint64_t entries = build_desc(specs[i], (int)s->n, blob.data() + offs[i], &pi.feat, &ntiles, &tile);
+    pi.K = specs[i].K;
+    pi.cls = specs[i].cls;
+    pi.desc_off = offs[i];
+    pi.tile_entries = tile;
+    pi.bytes = (double)entries * 2.0 * (double)esize(s);
+    pi.nbasic = specs[i].nbasic;
+    const int bps = pass_blocks_per_sm(pi.K, pi.cls, s->fp32);
+    const uint64_t cap = (uint64_t)s->sms * (uint64_t)bps;
+    pi.grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, cap));
+    s->passes.push_back(pi);
+  }
+  if (total > 0) {
+    DM_CUDA(cudaMalloc(&s->d_desc, total));
+    DM_CUDA(cudaMemcpyAsync(s->d_desc, blob.data(), total, cudaMemcpyHostToDevice, s->stream));
+    DM_CUDA(cudaStreamSynchronize(s->stream));
+  }
+  s->desc_bytes = total;
+  // capture the pass sequence once; run() replays it
+  if (s->graph_on && !s->passes.empty()) {
+    cudaGraph_t graph = nullptr;
+    DM_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      enqueue_passes(s, false);
+    } catch (...) {
+      cudaStreamEndCapture(s->stream, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    DM_CUDA(cudaStreamEndCapture(s->stream, &graph));
+    cudaError_t e = cudaGraphInstantiate(&s->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      s->gexec = nullptr;
+      throw DmError{DMSIM_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e)};
+    }
+  }
+  s->uploaded = true;
+}
+
+void run(dmsim_sim* s) {
+  if (!s->uploaded) throw DmError{DMSIM_ERR_STATE, "run() before upload()"};
+  ensure_state(s);
+  const bool timed = s->record != 0;
+  if (timed) {
+    for (PassInfo& p : s->passes) {
+      if (!p.ev0) DM_CUDA(cudaEventCreate(&p.ev0));
+      if (!p.ev1) DM_CUDA(cudaEventCreate(&p.ev1));
+    }
+  }
+  DM_CUDA(cudaEventRecord(s->ev0, s->stream));
+  if (timed || !s->gexec) enqueue_passes(s, timed);
+  else DM_CUDA(cudaGraphLaunch(s->gexec, s->stream));
+  DM_CUDA(cudaEventRecord(s->ev1, s->stream));
+  DM_CUDA(cudaEventSynchronize(s->ev1));
+  DM_CUDA(cudaGetLastError());
+  float ms = 0;
+  DM_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+  s->last_ms = ms;
+  double bytes = 0;
+  for (const PassInfo& p : s->passes) bytes += p.bytes;
+  s->last_bytes = bytes;
+  if (timed) {
+    s->records.clear();
+    for (const PassInfo& p : s->passes) {
+      float pms = 0;
+      DM_CUDA(cudaEventElapsedTime(&pms, p.ev0, p.ev1));
+      PassRecord r;
+      r.feat = p.feat;
+      r.ms = pms;
+      r.bytes = p.bytes;
+      s->records.push_back(r);
+    }
+  }
+  if (s->verbose) {
+    // the reference's per-run banner (PRINT_MEA_PER_CIRCUIT, :484-490)
+    const double mem = 2.0 * (double)s->N * (double)esize(s) / 1024.0 / 1024.0;
+    printf("\n============== DM-Sim ===============\n");
+    printf("nqubits:%u, ngates:%zu, ngpus:1, comp:%.3lf ms, comm:%.3lf ms, sim:%.3lf ms, mem:%.3lf MB, mem_per_gpu:%.3lf MB\n",
+           s->n, s->circuit.size(), (double)ms, 0.0, (double)ms, mem, mem);
+    printf("=====================================\n");
+  }
+}
+
+void clear_circuit(dmsim_sim* s) {
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (PassInfo& p : s->passes) {
+    if (p.ev0) cudaEventDestroy(p.ev0);
+    if (p.ev1) cudaEventDestroy(p.ev1);
+  }
+  free_plan(s);
+  s->circuit.clear();
+}
+
+void reset_dm(dmsim_sim* s) {
+  ensure_state(s);
+  DM_CUDA(launch_set_zero_state(s->d_re, s->d_im, s->N, s->fp32, s->stream));
+  DM_CUDA(cudaStreamSynchronize(s->stream));
+}
+
+std::vector<double> host_diag(dmsim_sim* s) {
+  ensure_state(s);
+  std::vector<double> d(s->dim);
+  DM_CUDA(launch_get_diag(s->d_re, s->dim, s->fp32, s->d_diag, s->stream));
+  DM_CUDA(cudaMemcpyAsync(d.data(), s->d_diag, s->dim * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  DM_CUDA(cudaStreamSynchronize(s->stream));
+  return d;
+}
+
+int fail(dmsim_sim* s, const DmError& e) {
+  if (s) s->err = e.msg;
+  return e.code;
+}
+
+}  // namespace
+
+// ============================================================================ C ABI
+#define DM_TRY(h, ...)                                                \
+  do {                                                                \
+    if (!(h)) return DMSIM_ERR_ARG;                                   \
+    try {                                                             \
+      __VA_ARGS__;                                                    \
+    } catch (const DmError& e_) {                                     \
+      return fail((h), e_);                                           \
+    } catch (const std::bad_alloc&) {                                 \
+      return fail((h), DmError{DMSIM_ERR_OOM, "host allocation failed"}); \
+    } catch (...) {                                                   \
+      return fail((h), DmError{DMSIM_ERR_ARG, "unexpected exception"}); \
+    }                                                                 \
+    (h)->err.clear();                                                 \
+    return DMSIM_OK;                                                  \
+  } while (0)
+
+extern "C" {
+
+int dmsim_create(uint32_t n_qubits, uint32_t n_gpus, dmsim_handle* out) {
+  if (!out) return DMSIM_ERR_ARG;
+  *out = nullptr;
+  // the reference requires n_gpus to be a power of 2 (:218-229); this engine
+  // is one GPU by design
+  if (n_gpus != 1) return DMSIM_ERR_UNSUPPORTED;
+  if (n_qubits < 1 || n_qubits > 17) return DMSIM_ERR_ARG;
+  dmsim_sim* s = new (std::nothrow) dmsim_sim;
+  if (!s) return DMSIM_ERR_OOM;
+  s->n = n_qubits;
+  s->dim = 1ull << n_qubits;
+  s->N = s->dim * s->dim;
+  try {
+    DM_CUDA(cudaGetDevice(&s->device));
+    DM_CUDA(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device));
+    DM_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    DM_CUDA(cudaEventCreate(&s->ev0));
+    DM_CUDA(cudaEventCreate(&s->ev1));
+    DM_CUDA(cudaMalloc(&s->d_diag, s->dim * sizeof(double)));
+    DM_CUDA(cudaMalloc(&s->d_acc, 8 * sizeof(double)));
+    // rho is allocated on first use so that complex64 can be chosen first
+    // (17 qubits fit only in complex64); FP64 up to 16 qubits is allocated now
+    if (n_qubits <= 16) ensure_state(s);
+  } catch (const DmError& e) {
+    int code = e.code;
+    dmsim_destroy(s);
+    return code;
+  }
+  *out = s;
+  return DMSIM_OK;
+}
+
+int dmsim_destroy(dmsim_handle s) {
+  if (!s) return DMSIM_ERR_ARG;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  clear_circuit(s);
+  free_state(s);
+  if (s->d_diag) cudaFree(s->d_diag);
+  if (s->d_acc) cudaFree(s->d_acc);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return DMSIM_OK;
+}
+
+int dmsim_set_option(dmsim_handle s, int key, int64_t v) {
+  DM_TRY(s, {
+    switch (key) {
+      case DMSIM_OPT_MODE:
+        if (v != 0 && v != 1) throw DmError{DMSIM_ERR_ARG, "mode must be 0 or 1"};
+        if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set the mode before upload()"};
+        s->mode = (int)v;
+        break;
+      case DMSIM_OPT_PRECISION: {
+        if (v != 0 && v != 1) throw DmError{DMSIM_ERR_ARG, "precision must be 0 (FP64) or 1 (complex64)"};
+        if (s->uploaded || !s->circuit.empty())
+          throw DmError{DMSIM_ERR_STATE, "set the precision before appending gates"};
+        if ((v == 1) != s->fp32) {
+          free_state(s);
+          s->fp32 = v == 1;
+        }
+        break;
+      }
+      case DMSIM_OPT_MAX_K:
+        if (v < 1 || v > kMaxK) throw DmError{DMSIM_ERR_ARG, "max_k must be 1..4"};
+        if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set max_k before upload()"};
+        s->maxk = (int)v;
+        break;
+      case DMSIM_OPT_PLANNER:
+        if (v != 0 && v != 1) throw DmError{DMSIM_ERR_ARG, "planner must be 0 or 1"};
+        if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set the planner before upload()"};
+        s->planner = (int)v;
+        break;
+      case DMSIM_OPT_RECORD: s->record = v != 0; break;
+      case DMSIM_OPT_SEED: s->seed = v; break;
+      case DMSIM_OPT_GRAPH:
+        if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set graph replay before upload()"};
+        s->graph_on = v != 0;
+        break;
+      case DMSIM_OPT_VERBOSE: s->verbose = v != 0; break;
+      default: throw DmError{DMSIM_ERR_ARG, "unknown option"};
+    }
+  });
+}
+
+int dmsim_get_option(dmsim_handle s, int key, int64_t* v) {
+  DM_TRY(s, {
+    if (!v) throw DmError{DMSIM_ERR_ARG, "null output"};
+    switch (key) {
+      case DMSIM_OPT_MODE: *v = s->mode; break;
+      case DMSIM_OPT_PRECISION: *v = s->fp32 ? 1 : 0; break;
+      case DMSIM_OPT_MAX_K: *v = s->maxk; break;
+      case DMSIM_OPT_PLANNER: *v = s->planner; break;
+      case DMSIM_OPT_RECORD: *v = s->record; break;
+      case DMSIM_OPT_SEED: *v = s->seed; break;
+      case DMSIM_OPT_GRAPH: *v = s->graph_on; break;
+      case DMSIM_OPT_VERBOSE: *v = s->verbose; break;
+      default: throw DmError{DMSIM_ERR_ARG, "unknown option"};
+    }
+  });
+}
+
+int dmsim_append(dmsim_handle s, int op, const uint32_t qb[5], double theta, double phi, double lambda) {
+  DM_TRY(s, {
+    if (!qb) throw DmError{DMSIM_ERR_ARG, "null qubit array"};
+    if (op < 0 || op >= N_REF_OPS) throw DmError{DMSIM_ERR_ARG, "unknown gate id " + std::to_string(op)};
+    GateRec g;
+    std::memset(&g, 0, sizeof g);
+    g.op = op;
+    for (int i = 0; i < 5; i++) g.qb[i] = qb[i];
+    g.theta = theta;
+    g.phi = phi;
+    g.lambda = lambda;
+    check_qubits(s, g);
+    s->circuit.push_back(g);
+  });
+}
+
+int dmsim_append_c1(dmsim_handle s, uint32_t q, const double m[8]) {
+  DM_TRY(s, {
+    if (!m) throw DmError{DMSIM_ERR_ARG, "null matrix"};
+    GateRec g;
+    std::memset(&g, 0, sizeof g);
+    g.op = OP_C1;
+    g.qb[0] = q;
+    std::memcpy(g.m, m, 8 * sizeof(double));
+    check_qubits(s, g);
+    s->circuit.push_back(g);
+  });
+}
+
+int dmsim_append_c2(dmsim_handle s, uint32_t q1, uint32_t q2, const double m[32]) {
+  DM_TRY(s, {
+    if (!m) throw DmError{DMSIM_ERR_ARG, "null matrix"};
+    GateRec g;
+    std::memset(&g, 0, sizeof g);
+    g.op = OP_C2;
+    g.qb[0] = q1;
+    g.qb[1] = q2;
+    std::memcpy(g.m, m, 32 * sizeof(double));
+    check_qubits(s, g);
+    s->circuit.push_back(g);
+  });
+}
+
+int dmsim_upload(dmsim_handle s) { DM_TRY(s, upload(s)); }
+int dmsim_run(dmsim_handle s) { DM_TRY(s, run(s)); }
+int dmsim_clear_circuit(dmsim_handle s) { DM_TRY(s, clear_circuit(s)); }
+int dmsim_reset_dm(dmsim_handle s) { DM_TRY(s, reset_dm(s)); }
+int dmsim_reset(dmsim_handle s) {
+  DM_TRY(s, {
+    clear_circuit(s);
+    reset_dm(s);
+  });
+}
+
+int dmsim_measure(dmsim_handle s, uint32_t rep, const double* uniforms, uint64_t* out) {
+  DM_TRY(s, {
+    if (!out && rep) throw DmError{DMSIM_ERR_ARG, "null output"};
+    const std::vector<double> d = host_diag(s);
+    // sequential FP64 prefix of |Re rho_ii| (:527-533)
+    std::vector<double> scan(s->dim + 1);
+    scan[0] = 0;
+    for (uint64_t i = 1; i < s->dim + 1; i++) scan[i] = scan[i - 1] + std::fabs(d[i - 1]);
+    std::vector<double> u(rep);
+    if (uniforms) {
+      std::memcpy(u.data(), uniforms, rep * sizeof(double));
+    } else {
+      // srand(RAND_SEED) + rand()/RAND_MAX (:534-538), RAND_SEED = time(0) by default
+      srand(s->seed >= 0 ? (unsigned)s->seed : (unsigned)time(0));
+      for (uint32_t i = 0; i < rep; i++) u[i] = (double)rand() / (double)RAND_MAX;
+    }
+    for (uint32_t i = 0; i < rep; i++) {
+      // the reference's linear search returns the j with scan[j] <= r <
+      // scan[j+1] (0 if none); scan is non-decreasing, so that j is the one
+      // before the first entry greater than r.
+      const double r = u[i];
+      const auto it = std::upper_bound(scan.begin(), scan.end(), r);
+      uint64_t res = 0;
+      if (it != scan.begin() && it != scan.end()) res = (uint64_t)(it - scan.begin()) - 1;
+      out[i] = res;
+    }
+    if (std::fabs(scan[s->dim] - 1.0) > 1e-3)  // ERROR_BAR (src/config.hpp:53)
+      fprintf(stderr, "Sum of probability along diag is far from 1.0 with %lf\n", scan[s->dim]);
+  });
+}
+
+int dmsim_get_dm(dmsim_handle s, double* re, double* im) {
+  DM_TRY(s, {
+    if (!re || !im) throw DmError{DMSIM_ERR_ARG, "null buffer"};
+    ensure_state(s);
+    if (!s->fp32) {
+      DM_CUDA(cudaMemcpyAsync(re, s->d_re, s->N * 8, cudaMemcpyDeviceToHost, s->stream));
+      DM_CUDA(cudaMemcpyAsync(im, s->d_im, s->N * 8, cudaMemcpyDeviceToHost, s->stream));
+      DM_CUDA(cudaStreamSynchronize(s->stream));
+    } else {
+      std::vector<float> tmp(s->N);
+      DM_CUDA(cudaMemcpy(tmp.data(), s->d_re, s->N * 4, cudaMemcpyDeviceToHost));
+      for (uint64_t i = 0; i < s->N; i++) re[i] = tmp[i];
+      DM_CUDA(cudaMemcpy(tmp.data(), s->d_im, s->N * 4, cudaMemcpyDeviceToHost));
+      for (uint64_t i = 0; i < s->N; i++) im[i] = tmp[i];
+    }
+  });
+}
+
+int dmsim_set_dm(dmsim_handle s, const double* re, const double* im) {
+  DM_TRY(s, {
+    if (!re || !im) throw DmError{DMSIM_ERR_ARG, "null buffer"};
+    ensure_state(s);
+    if (!s->fp32) {
+      DM_CUDA(cudaMemcpyAsync(s->d_re, re, s->N * 8, cudaMemcpyHostToDevice, s->stream));
+      DM_CUDA(cudaMemcpyAsync(s->d_im, im, s->N * 8, cudaMemcpyHostToDevice, s->stream));
+      DM_CUDA(cudaStreamSynchronize(s->stream));
+    } else {
+      std::vector<float> tmp(s->N);
+      for (uint64_t i = 0; i < s->N; i++) tmp[i] = (float)re[i];
+      DM_CUDA(cudaMemcpy(s->d_re, tmp.data(), s->N * 4, cudaMemcpyHostToDevice));
+      for (uint64_t i = 0; i < s->N; i++) tmp[i] = (float)im[i];
+      DM_CUDA(cudaMemcpy(s->d_im, tmp.data(), s->N * 4, cudaMemcpyHostToDevice));
+    }
+  });
+}
+
+int dmsim_get_diag(dmsim_handle s, double* diag) {
+  DM_TRY(s, {
+    if (!diag) throw DmError{DMSIM_ERR_ARG, "null buffer"};
+    const std::vector<double> d = host_diag(s);
+    std::memcpy(diag, d.data(), s->dim * sizeof(double));
+  });
+}
+
+int dmsim_dump(dmsim_handle s, char* buf, size_t len, size_t* needed) {
+  DM_TRY(s, {
+    // Gate::dump (:170-176): NAME(qb0,qb1,qb2,qb3,qb4,theta,phi,lambda);
+    std::stringstream ss;
+    for (const GateRec& g : s->circuit) {
+      const char* name = g.op == OP_C1 ? "C1" : g.op == OP_C2 ? "C2" : kOpNames[g.op];
+      ss << name << "(" << g.qb[0] << "," << g.qb[1] << "," << g.qb[2] << "," << g.qb[3] << "," << g.qb[4] << ","
+         << g.theta << "," << g.phi << "," << g.lambda << ");" << std::endl;
+    }
+    const std::string str = ss.str();
+    if (needed) *needed = str.size() + 1;
+    if (buf && len > 0) {
+      const size_t c = std::min(len - 1, str.size());
+      std::memcpy(buf, str.data(), c);
+      buf[c] = 0;
+    }
+  });
+}
+
+int dmsim_n_qubits(dmsim_handle s, uint32_t* n) {
+  DM_TRY(s, {
+    if (!n) throw DmError{DMSIM_ERR_ARG, "null output"};
+    *n = s->n;
+  });
+}
+
+int dmsim_n_gates(dmsim_handle s, uint32_t* n) {
+  DM_TRY(s, {
+    if (!n) throw DmError{DMSIM_ERR_ARG, "null output"};
+    *n = (uint32_t)s->circuit.size();
+  });
+}
+
+int dmsim_plan_stats(dmsim_handle s, uint32_t* n_passes, uint32_t* n_basic) {
+  DM_TRY(s, {
+    if (n_passes) *n_passes = (uint32_t)s->passes.size();
+    if (n_basic) *n_basic = s->n_basic;
+  });
+}
+
+int dmsim_last_timings(dmsim_handle s, double out[3]) {
+  DM_TRY(s, {
+    if (!out) throw DmError{DMSIM_ERR_ARG, "null output"};
+    out[0] = s->last_ms;
+    out[1] = (double)s->passes.size();
+    out[2] = s->last_bytes;
+  });
+}
+
+int dmsim_pass_records(dmsim_handle s, double* out, uint32_t cap, uint32_t* count) {
+  DM_TRY(s, {
+    if (count) *count = (uint32_t)s->records.size();
+    if (out)
+      for (uint32_t i = 0; i < cap && i < s->records.size(); i++) {
+        const PassRecord& r = s->records[i];
+        double* o = out + 8 * i;
+        o[0] = r.feat.K;
+        o[1] = r.feat.cls;
+        o[2] = r.feat.nnz;
+        o[3] = r.feat.max_lo_bit;
+        o[4] = r.feat.min_hi_bit;
+        o[5] = r.feat.n;
+        o[6] = r.ms;
+        o[7] = r.bytes;
+      }
+  });
+}
+
+int dmsim_pure_metrics(dmsim_handle s, const double* psi_re, const double* psi_im, double out[4]) {
+  DM_TRY(s, {
+    if (!psi_re || !psi_im || !out) throw DmError{DMSIM_ERR_ARG, "null buffer"};
+    ensure_state(s);
+    double* d_psi = nullptr;
+    DM_CUDA(cudaMalloc(&d_psi, 2 * s->dim * sizeof(double)));
+    cudaError_t e = cudaMemcpyAsync(d_psi, psi_re, s->dim * 8, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_psi + s->dim, psi_im, s->dim * 8, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = launch_pure_metrics(s->d_re, s->d_im, s->fp32, d_psi, d_psi + s->dim, (int)s->n, s->d_acc, s->sms, s->stream);
+    double acc[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(acc, s->d_acc, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(d_psi);
+    if (e != cudaSuccess) throw DmError{DMSIM_ERR_CUDA, std::string("pure_metrics: ") + cudaGetErrorString(e)};
+    out[0] = acc[0];
+    out[1] = acc[1];
+    out[2] = std::sqrt(acc[2]);
+    out[3] = std::sqrt(acc[3]);
+  });
+}
+
+int dmsim_compare_states(dmsim_handle a, dmsim_handle b, double out[2]) {
+  DM_TRY(a, {
+    if (!b || !out) throw DmError{DMSIM_ERR_ARG, "null argument"};
+    if (a->N != b->N || a->fp32 != b->fp32) throw DmError{DMSIM_ERR_ARG, "states differ in size or precision"};
+    ensure_state(a);
+    ensure_state(b);
+    DM_CUDA(cudaStreamSynchronize(b->stream));
+    DM_CUDA(launch_compare(a->d_re, a->d_im, b->d_re, b->d_im, a->fp32, a->N, a->d_acc, a->sms, a->stream));
+    double acc[2] = {0, 0};
+    DM_CUDA(cudaMemcpyAsync(acc, a->d_acc, 2 * sizeof(double), cudaMemcpyDeviceToHost, a->stream));
+    DM_CUDA(cudaStreamSynchronize(a->stream));
+    out[0] = std::sqrt(acc[0]);
+    out[1] = std::sqrt(acc[1]);
+  });
+}
+
+int dmsim_alloc_host(size_t bytes, void** out) {
+  if (!out) return DMSIM_ERR_ARG;
+  *out = nullptr;
+  cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    return e == cudaErrorMemoryAllocation ? DMSIM_ERR_OOM : DMSIM_ERR_CUDA;
+  }
+  return DMSIM_OK;
+}
+
+int dmsim_free_host(void* p) {
+  if (!p) return DMSIM_ERR_ARG;
+  return cudaFreeHost(p) == cudaSuccess ? DMSIM_OK : DMSIM_ERR_CUDA;
+}
+
+int dmsim_device_state(dmsim_handle s, void** re, void** im) {
+  DM_TRY(s, {
+    ensure_state(s);
+    if (re) *re = s->d_re;
+    if (im) *im = s->d_im;
+  });
+}
+
+int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qubits, const double* params,
+                       const double* mats, uint32_t ngates, int mode, int max_k, int planner, double* out, uint32_t cap,
+                       uint32_t* npasses) {
+  if (!ops || !qubits || !params || n_qubits < 1 || n_qubits > 30 || max_k < 1 || max_k > kMaxK) return DMSIM_ERR_ARG;
+  try {
+    std::vector<Basic> basics;
+    for (uint32_t i = 0; i < ngates; i++) {
+      GateRec g;
+      std::memset(&g, 0, sizeof g);
+      g.op = ops[i];
+      for (int k = 0; k < 5; k++) g.qb[k] = qubits[5 * i + k];
+      g.theta = params[3 * i];
+      g.phi = params[3 * i + 1];
+      g.lambda = params[3 * i + 2];
+      if (mats) std::memcpy(g.m, mats + 32 * i, 32 * sizeof(double));
+      const int ar = gate_arity(g.op);
+      if (ar == 0) return DMSIM_ERR_ARG;
+      for (int k = 0; k < ar; k++)
+        if (g.qb[k] >= n_qubits) return DMSIM_ERR_ARG;
+      decompose(g, basics);
+    }
+    std::vector<PassSpec> specs;
+    if (mode == 0) specs = plan_plain(basics);
+    else if (planner == 1) return DMSIM_ERR_UNSUPPORTED;
+    else specs = plan_greedy(basics, max_k);
+    if (npasses) *npasses = (uint32_t)specs.size();
+    if (out)
+      for (uint32_t i = 0; i < cap && i < specs.size(); i++) {
+        const PassSpec& p = specs[i];
+        double* o = out + (size_t)DMSIM_PASS_REC * i;
+        std::memset(o, 0, DMSIM_PASS_REC * sizeof(double));
+        o[0] = p.K;
+        o[1] = p.cls;
+        o[2] = p.nbasic;
+        o[3] = p.nnz;
+        for (int k = 0; k < p.K; k++) o[4 + k] = p.q[k];
+        if (p.rlin) {
+          std::memcpy(o + 8, p.rl, 16 * sizeof(double));
+          std::memcpy(o + 24, p.rlb, 16 * sizeof(double));
+        } else {
+          const int D = 1 << p.K;
+          for (int j = 0; j < D * D; j++) {
+            o[8 + 2 * j] = p.U[j].real();
+            o[8 + 2 * j + 1] = p.U[j].imag();
+          }
+        }
+      }
+  } catch (...) {
+    return DMSIM_ERR_ARG;
+  }
+  return DMSIM_OK;
+}
+
+const char* dmsim_last_error(dmsim_handle s) { return s ? s->err.c_str() : "null handle"; }
+
+const char* dmsim_status_string(int st) {
+  switch (st) {
+    case DMSIM_OK: return "ok";
+    case DMSIM_ERR_ARG: return "invalid argument";
+    case DMSIM_ERR_STATE: return "call out of order";
+    case DMSIM_ERR_OOM: return "out of memory";
+    case DMSIM_ERR_CUDA: return "CUDA error";
+    case DMSIM_ERR_TIMEOUT: return "device wait timed out";
+    case DMSIM_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,27 @@
+// engine_internal.h -- per-pass bookkeeping shared inside the engine.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "plan.h"
+
+namespace dmg {
+
+struct PassInfo {
+  int K, cls;
+  size_t desc_off;      // byte offset of the descriptor in the device blob
+  int tile_entries;
+  unsigned grid;
+  double bytes;         // algorithmic bytes moved (reads + writes)
+  int nbasic;
+  PassFeatures feat;
+  cudaEvent_t ev0, ev1; // per-pass timing (record mode)
+};
+
+struct PassRecord {
+  PassFeatures feat;
+  double ms;
+  double bytes;
+};
+
+}  // namespace dmg

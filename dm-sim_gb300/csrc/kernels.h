@@ -1,0 +1,27 @@
+// kernels.h -- host-side entry points of the pass kernels (kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace dmg {
+
+struct LaunchArgs {
+  void* re;            // device real parts (double or float)
+  void* im;            // device imaginary parts
+  const void* desc;    // device PassDesc<K>
+  int K, cls;
+  bool fp32;
+  unsigned grid;       // blocks
+  int tile_entries;    // G * 4^K
+};
+
+// Launch one pass on stream s.
+cudaError_t launch_pass(const LaunchArgs& a, cudaStream_t s);
+// Resident blocks per SM of the kernel instance for (K, cls, precision).
+int pass_blocks_per_sm(int K, int cls, bool fp32);
+// rho <- |0..0><0..0|
+cudaError_t launch_set_zero_state(void* re, void* im, uint64_t N, bool fp32, cudaStream_t s);
+// d_out[i] = Re rho[i][i] (FP64 whatever the state precision)
+cudaError_t launch_get_diag(const void* re, uint64_t dim, bool fp32, double* d_out, cudaStream_t s);
+
+}  // namespace dmg

@@ -1,0 +1,117 @@
+// metrics.cu -- comparison of the device density matrix with a pure state.
+//
+// For rho held as A[c*2^n + r] = rho[r][c] and a pure state psi, one pass
+// over A gives the fidelity <psi|rho|psi> = sum_{r,c} conj(psi_r) rho[r][c]
+// psi_c, the trace, the largest |rho[r][c] - psi_r conj(psi_c)| and the
+// Frobenius norm of the difference.  These back the full-size parity checks,
+// where the CPU density-matrix oracle cannot run, with the statevector oracle.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "metrics.h"
+
+namespace dmg {
+
+__device__ __forceinline__ void atomic_max_nonneg(double* addr, double v) {
+  // non-negative doubles order like their bit patterns
+  atomicMax(reinterpret_cast<unsigned long long*>(addr), (unsigned long long)__double_as_longlong(v));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_pure_metrics(const T* __restrict__ re, const T* __restrict__ im,
+                                                      const double* __restrict__ pr, const double* __restrict__ pi,
+                                                      int n, double* acc) {
+  const uint64_t dim = 1ull << n, N = dim * dim;
+  double fid = 0, tr = 0, mx = 0, fro = 0;
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < N; v += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t r = v & (dim - 1), c = v >> n;
+    const double ar = (double)re[v], ai = (double)im[v];
+    // psi_r conj(psi_c)
+    const double er = pr[r] * pr[c] + pi[r] * pi[c];
+    const double ei = pi[r] * pr[c] - pr[r] * pi[c];
+    const double dr = ar - er, di = ai - ei;
+    const double d2 = dr * dr + di * di;
+    fro += d2;
+    mx = fmax(mx, d2);
+    // conj(psi_r) * A * psi_c, real part
+    const double tr_ = pr[r] * ar + pi[r] * ai;  // conj(psi_r) * A
+    const double ti_ = pr[r] * ai - pi[r] * ar;
+    fid += tr_ * pr[c] - ti_ * pi[c];
+    if (r == c) tr += ar;
+  }
+  __shared__ double s[4][256];
+  s[0][threadIdx.x] = fid;
+  s[1][threadIdx.x] = tr;
+  s[2][threadIdx.x] = mx;
+  s[3][threadIdx.x] = fro;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      s[0][threadIdx.x] += s[0][threadIdx.x + st];
+      s[1][threadIdx.x] += s[1][threadIdx.x + st];
+      s[2][threadIdx.x] = fmax(s[2][threadIdx.x], s[2][threadIdx.x + st]);
+      s[3][threadIdx.x] += s[3][threadIdx.x + st];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    atomicAdd(&acc[0], s[0][0]);
+    atomicAdd(&acc[1], s[1][0]);
+    atomic_max_nonneg(&acc[2], s[2][0]);
+    atomicAdd(&acc[3], s[3][0]);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_compare(const T* __restrict__ ar, const T* __restrict__ ai,
+                                                 const T* __restrict__ br, const T* __restrict__ bi, uint64_t N,
+                                                 double* acc) {
+  double mx = 0, fro = 0;
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < N; v += (uint64_t)gridDim.x * blockDim.x) {
+    const double dr = (double)ar[v] - (double)br[v], di = (double)ai[v] - (double)bi[v];
+    const double d2 = dr * dr + di * di;
+    fro += d2;
+    mx = fmax(mx, d2);
+  }
+  __shared__ double s[2][256];
+  s[0][threadIdx.x] = mx;
+  s[1][threadIdx.x] = fro;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      s[0][threadIdx.x] = fmax(s[0][threadIdx.x], s[0][threadIdx.x + st]);
+      s[1][threadIdx.x] += s[1][threadIdx.x + st];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    atomic_max_nonneg(&acc[0], s[0][0]);
+    atomicAdd(&acc[1], s[1][0]);
+  }
+}
+
+cudaError_t launch_compare(const void* ar, const void* ai, const void* br, const void* bi, bool fp32, uint64_t N,
+                           double* d_acc, int sms, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(d_acc, 0, 2 * sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  const unsigned grid = (unsigned)(sms * 4);
+  if (fp32)
+    k_compare<float><<<grid, 256, 0, s>>>((const float*)ar, (const float*)ai, (const float*)br, (const float*)bi, N, d_acc);
+  else
+    k_compare<double><<<grid, 256, 0, s>>>((const double*)ar, (const double*)ai, (const double*)br, (const double*)bi, N, d_acc);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pure_metrics(const void* re, const void* im, bool fp32, const double* psi_re, const double* psi_im,
+                                int n, double* d_acc, int sms, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(d_acc, 0, 4 * sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  const unsigned grid = (unsigned)(sms * 4);
+  if (fp32)
+    k_pure_metrics<float><<<grid, 256, 0, s>>>((const float*)re, (const float*)im, psi_re, psi_im, n, d_acc);
+  else
+    k_pure_metrics<double><<<grid, 256, 0, s>>>((const double*)re, (const double*)im, psi_re, psi_im, n, d_acc);
+  return cudaGetLastError();
+}
+
+}  // namespace dmg

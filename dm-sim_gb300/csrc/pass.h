@@ -1,0 +1,73 @@
+// pass.h -- one superoperator pass over the vectorised density matrix.
+//
+// The state is the 4^n-entry array A with A[c*2^n + r] = rho[r][c]: the layout
+// of DM-Sim's dm_real_res/dm_imag_res after sim() (src/dmsim_nvgpu_omp.cuh:
+// 456-459), held as separate real and imaginary arrays.  Ket qubit q is bit q
+// of the index and bra qubit q is bit q+n.  A pass applies a K-qubit operator
+// U (K <= 4) as U (x) conj(U) on bits {q_i} and {q_i + n} in place.
+//
+// Tiling.  A tile is the closed set of G * 4^K entries (G = 256/2^K groups)
+// that the operator mixes, chosen so that it is made of 2^mhi contiguous runs
+// of 2^L entries: the low L index bits (which hold the low target bits plus
+// log2(G) free bits) are contiguous in memory and the mhi target bits at or
+// above L select the run.  Loads and stores of a run are coalesced 16-byte
+// vector accesses whatever qubits the pass targets.
+#pragma once
+#include <stdint.h>
+
+namespace dmg {
+
+constexpr int kThreads = 256;  // threads per block of every pass kernel
+constexpr int kMaxK = 4;       // widest fused operator
+constexpr int kMaxD = 16;      // 2^kMaxK
+
+// Arithmetic class of a pass; selects the kernel instance.
+enum PassClass : int32_t {
+  CLS_MOVE = 0,    // monomial superoperator, every factor exactly 1 (X, CX, SWAP, Toffoli blocks)
+  CLS_SIGNED = 1,  // monomial, factors in {1,-1,+i,-i}: sign and re/im swaps only (Y, Z, S, CZ)
+  CLS_PHASE = 2,   // monomial with general complex factors (T, U1, controlled phases)
+  CLS_DENSE = 3,   // general U, applied ket side then bra side (dense rows)
+  CLS_SPARSE = 4,  // general U with sparse rows (per-row column lists)
+  CLS_RLIN = 5,    // real-linear 1-qubit map (DM-Sim's SRN gate), K = 1
+  CLS_COUNT = 6
+};
+
+// Factor kinds of a monomial superoperator entry f[a][b].
+enum FactorKind : int8_t { FK_ONE = 0, FK_NEG = 1, FK_PI = 2, FK_NI = 3, FK_GEN = 4 };
+
+struct PassHeader {
+  int32_t K, cls;
+  int32_t L;         // low run bits
+  int32_t mhi;       // number of target bits >= L
+  int32_t g;         // log2 of groups per tile
+  int32_t pad;
+  uint64_t ntiles;   // tiles in the state
+  int32_t hipos[8];  // global positions of the high target bits, ascending
+  int32_t lket[4];   // local bit position of ket target i (qubit q_i)
+  int32_t lbra[4];   // local bit position of bra target i (bit q_i + n)
+  int32_t freepos[8];// local positions of the g free low bits, ascending
+  uint32_t ldmask[8];   // bit h set: run h is read (it holds a source of a stored entry)
+  uint32_t stmask[8];   // bit h set: run h is written (it holds an entry the pass changes)
+};
+
+// Operator payload for width K (D = 2^K).
+template <int K>
+struct PassOp {
+  static constexpr int D = 1 << K;
+  double ure[D * D], uim[D * D];   // U row-major (DENSE/SPARSE)
+  double fre[D * D], fim[D * D];   // f[a*D+b] = p_a * conj(p_b) (PHASE)
+  double rlin[16];                 // RLIN: ket 4x4 real map on (r0,i0,r1,i1); rlin-bar follows
+  double rlinb[16];
+  int8_t nnz[D];                   // SPARSE: nonzeros per row
+  int8_t col[D * D];               // SPARSE: column list per row
+  int8_t src[D];                   // monomial: source index of row a (U[a][src[a]] != 0)
+  int8_t fk[D * D];                // monomial: factor kind of f[a][b]
+};
+
+template <int K>
+struct PassDesc {
+  PassHeader h;
+  PassOp<K> op;
+};
+
+}  // namespace dmg

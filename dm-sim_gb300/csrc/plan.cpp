@@ -1,0 +1,428 @@
+// plan.cpp -- pass construction and the fixed-width fusion planner.
+#include "plan.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace dmg {
+
+// ---------------------------------------------------------------- fusion
+namespace {
+
+// Left-multiply the D x D group matrix U (qubit list qs) by basic gate b.
+void apply_basic(cplx* U, int K, const int* qs, const Basic& b) {
+  const int D = 1 << K;
+  auto pos = [&](int q) {
+    for (int i = 0; i < K; i++)
+      if (qs[i] == q) return i;
+    return -1;
+  };
+  if (b.kind == BK_1Q) {
+    const int i = pos(b.q[0]);
+    const int m = 1 << i;
+    for (int c = 0; c < D; c++)
+      for (int r0 = 0; r0 < D; r0++) {
+        if (r0 & m) continue;
+        const int r1 = r0 | m;
+        const cplx x0 = U[r0 * D + c], x1 = U[r1 * D + c];
+        U[r0 * D + c] = b.u[0] * x0 + b.u[1] * x1;
+        U[r1 * D + c] = b.u[2] * x0 + b.u[3] * x1;
+      }
+  } else {  // BK_2Q: sub-index j = bit(q[0]) + 2 bit(q[1])
+    const int i0 = pos(b.q[0]), i1 = pos(b.q[1]);
+    const int m0 = 1 << i0, m1 = 1 << i1;
+    for (int c = 0; c < D; c++)
+      for (int r = 0; r < D; r++) {
+        if ((r & m0) || (r & m1)) continue;
+        const int rr[4] = {r, r | m0, r | m1, r | m0 | m1};
+        cplx x[4];
+        for (int j = 0; j < 4; j++) x[j] = U[rr[j] * D + c];
+        for (int j = 0; j < 4; j++) {
+          cplx acc = 0;
+          for (int k = 0; k < 4; k++) acc += b.u[j * 4 + k] * x[k];
+          U[rr[j] * D + c] = acc;
+        }
+      }
+  }
+}
+
+int nq(const Basic& b) { return b.kind == BK_2Q ? 2 : 1; }
+
+PassSpec single(const Basic& b) {
+  PassSpec p;
+  p.nbasic = 1;
+  if (b.kind == BK_RLIN) {
+    p.K = 1;
+    p.q[0] = b.q[0];
+    p.rlin = true;
+    std::memcpy(p.rl, b.rl, sizeof p.rl);
+    std::memcpy(p.rlb, b.rlb, sizeof p.rlb);
+    p.cls = CLS_RLIN;
+    return p;
+  }
+  p.K = nq(b);
+  p.q[0] = b.q[0];
+  if (p.K == 2) p.q[1] = b.q[1];
+  const int D = 1 << p.K;
+  for (int i = 0; i < D * D; i++) p.U[i] = b.u[i];
+  classify(p, false);
+  return p;
+}
+
+}  // namespace
+
+std::vector<PassSpec> plan_plain(const std::vector<Basic>& basics) {
+  std::vector<PassSpec> out;
+  out.reserve(basics.size());
+  for (const Basic& b : basics) out.push_back(single(b));
+  return out;
+}
+
+std::vector<PassSpec> plan_greedy(const std::vector<Basic>& basics, int maxk) {
+  std::vector<PassSpec> out;
+  const int m = (int)basics.size();
+  if (maxk < 1) maxk = 1;
+  if (maxk > kMaxK) maxk = kMaxK;
+  // per-qubit program order
+  int nqb = 0;
+  for (const Basic& b : basics) nqb = std::max(nqb, std::max(b.q[0], b.q[1]) + 1);
+  std::vector<std::vector<int>> qlist(nqb);
+  for (int i = 0; i < m; i++) {
+    qlist[basics[i].q[0]].push_back(i);
+    if (nq(basics[i]) == 2) qlist[basics[i].q[1]].push_back(i);
+  }
+  std::vector<int> head(nqb, 0);
+  std::vector<char> taken(m, 0);
+  auto is_front = [&](int j) {
+    const Basic& b = basics[j];
+    if (qlist[b.q[0]][head[b.q[0]]] != j) return false;
+    if (nq(b) == 2 && qlist[b.q[1]][head[b.q[1]]] != j) return false;
+    return true;
+  };
+  auto take = [&](int j) {
+    taken[j] = 1;
+    head[basics[j].q[0]]++;
+    if (nq(basics[j]) == 2) head[basics[j].q[1]]++;
+  };
+  const int kWindow = 96;  // look-ahead over untaken gates
+  int first = 0;
+  while (first < m) {
+    while (first < m && taken[first]) first++;
+    if (first >= m) break;
+    const Basic& b0 = basics[first];
+    if (b0.kind == BK_RLIN) {  // real-linear gates are fusion barriers
+      take(first);
+      out.push_back(single(b0));
+      continue;
+    }
+    int qs[kMaxK];
+    int K = 0;
+    qs[K++] = b0.q[0];
+    if (nq(b0) == 2) qs[K++] = b0.q[1];
+    if (K > maxk) {  // a 2-qubit gate with maxk == 1: its own pass
+      take(first);
+      out.push_back(single(b0));
+      continue;
+    }
+    std::vector<int> members{first};
+    take(first);
+    for (;;) {
+      int best = -1, best_new = 99;
+      int seen = 0;
+      for (int j = first + 1; j < m && seen < kWindow; j++) {
+        if (taken[j]) continue;
+        seen++;
+        const Basic& b = basics[j];
+        if (b.kind == BK_RLIN) continue;
+        if (!is_front(j)) continue;
+        int add = 0;
+        const int bq[2] = {b.q[0], b.q[1]};
+        for (int t = 0; t < nq(b); t++) {
+          bool in = false;
+          for (int i = 0; i < K; i++) in |= qs[i] == bq[t];
+          add += in ? 0 : 1;
+        }
+        if (K + add > maxk) continue;
+        if (add < best_new) {
+          best_new = add;
+          best = j;
+          if (add == 0) break;
+        }
+      }
+      if (best < 0) break;
+      const Basic& b = basics[best];
+      for (int t = 0; t < nq(b); t++) {
+        bool in = false;
+        for (int i = 0; i < K; i++) in |= qs[i] == b.q[t];
+        if (!in) qs[K++] = b.q[t];
+      }
+      members.push_back(best);
+      take(best);
+    }
+    if (members.size() == 1) {
+      out.push_back(single(basics[members[0]]));
+      continue;
+    }
+    PassSpec p;
+    p.K = K;
+    for (int i = 0; i < K; i++) p.q[i] = qs[i];
+    const int D = 1 << K;
+    for (int i = 0; i < D * D; i++) p.U[i] = (i / D == i % D) ? cplx(1, 0) : cplx(0, 0);
+    for (int j : members) apply_basic(p.U, K, qs, basics[j]);
+    p.nbasic = (int)members.size();
+    classify(p, true);
+    out.push_back(p);
+  }
+  return out;
+}
+
+// ---------------------------------------------------------------- classes
+namespace {
+// Entries within this distance of 0, +-1 are taken as exact.  Products of
+// up to a few hundred basic gates carry roundoff of order 1e-15; a fused
+// operator's structural zeros and ones are restored exactly so the kernel
+// can skip the arithmetic.
+constexpr double kSnapFused = 1e-13;
+// For a single basic gate only the superoperator factors are snapped (e.g.
+// |T11|^2 = 1 + 2e-16); the matrix entries are taken as given.
+constexpr double kSnapFactor = 1e-15;
+
+double snap1(double x, double eps) {
+  if (std::fabs(x) < eps) return 0.0;
+  if (std::fabs(x - 1.0) < eps) return 1.0;
+  if (std::fabs(x + 1.0) < eps) return -1.0;
+  return x;
+}
+}  // namespace
+
+void classify(PassSpec& p, bool fused) {
+  if (p.rlin) {
+    p.cls = CLS_RLIN;
+    p.nnz = 4;
+    return;
+  }
+  const int D = 1 << p.K;
+  if (fused)
+    for (int i = 0; i < D * D; i++) p.U[i] = cplx(snap1(p.U[i].real(), kSnapFused), snap1(p.U[i].imag(), kSnapFused));
+  int nnz = 0;
+  bool mono = true;
+  std::vector<int> colcount(D, 0);
+  for (int a = 0; a < D; a++) {
+    int rn = 0;
+    for (int c = 0; c < D; c++)
+      if (p.U[a * D + c] != cplx(0, 0)) {
+        rn++;
+        colcount[c]++;
+      }
+    nnz += rn;
+    if (rn != 1) mono = false;
+  }
+  for (int c = 0; c < D; c++)
+    if (colcount[c] != 1) mono = false;
+  p.nnz = nnz;
+  if (mono) {
+    bool all_one = true, all_signed = true;
+    for (int a = 0; a < D; a++) {
+      int sa = 0;
+      while (p.U[a * D + sa] == cplx(0, 0)) sa++;
+      for (int b = 0; b < D; b++) {
+        int sb = 0;
+        while (p.U[b * D + sb] == cplx(0, 0)) sb++;
+        const cplx f = p.U[a * D + sa] * std::conj(p.U[b * D + sb]);
+        const double fr = snap1(f.real(), kSnapFactor), fi = snap1(f.imag(), kSnapFactor);
+        const bool one = fr == 1.0 && fi == 0.0;
+        const bool sgn = one || (fr == -1.0 && fi == 0.0) || (fr == 0.0 && (fi == 1.0 || fi == -1.0));
+        all_one &= one;
+        all_signed &= sgn;
+      }
+    }
+    p.cls = all_one ? CLS_MOVE : (all_signed ? CLS_SIGNED : CLS_PHASE);
+    return;
+  }
+  p.cls = (4 * nnz > 3 * D * D) ? CLS_DENSE : CLS_SPARSE;
+}
+
+// ---------------------------------------------------------------- descriptors
+size_t desc_size(int K) {
+  switch (K) {
+    case 1: return sizeof(PassDesc<1>);
+    case 2: return sizeof(PassDesc<2>);
+    case 3: return sizeof(PassDesc<3>);
+    default: return sizeof(PassDesc<4>);
+  }
+}
+
+namespace {
+
+template <int K>
+uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, uint64_t* ntiles_out, int* tile_out) {
+  constexpr int D = 1 << K;
+  std::memset(d, 0, sizeof(*d));
+  PassHeader& h = d->h;
+  PassOp<K>& op = d->op;
+  const int nb = 2 * n;
+  h.K = K;
+  h.cls = p.cls;
+  // target bit positions
+  std::vector<int> P;
+  for (int i = 0; i < K; i++) {
+    P.push_back(p.q[i]);
+    P.push_back(p.q[i] + n);
+  }
+  std::sort(P.begin(), P.end());
+  std::vector<int> F;
+  for (int b = 0; b < nb; b++)
+    if (!std::binary_search(P.begin(), P.end(), b)) F.push_back(b);
+  int g = 8 - K;
+  if (g > (int)F.size()) g = (int)F.size();
+  // L: the position of the (g+1)-th free bit, so that exactly g free bits
+  // and every target bit below it lie in the contiguous low run.
+  const int L = (g < (int)F.size()) ? F[g] : nb;
+  std::vector<int> hi;
+  for (int x : P)
+    if (x >= L) hi.push_back(x);
+  h.g = g;
+  h.L = L;
+  h.mhi = (int)hi.size();
+  for (int j = 0; j < h.mhi; j++) h.hipos[j] = hi[j];
+  auto local = [&](int x) {
+    if (x < L) return x;
+    return L + (int)(std::lower_bound(hi.begin(), hi.end(), x) - hi.begin());
+  };
+  for (int i = 0; i < K; i++) {
+    h.lket[i] = local(p.q[i]);
+    h.lbra[i] = local(p.q[i] + n);
+  }
+  for (int j = 0; j < g; j++) h.freepos[j] = F[j];
+  h.ntiles = 1ull << (nb - L - h.mhi);
+
+  // operator tables
+  for (int i = 0; i < D * D; i++) {
+    op.ure[i] = p.U[i].real();
+    op.uim[i] = p.U[i].imag();
+  }
+  std::memcpy(op.rlin, p.rl, sizeof op.rlin);
+  std::memcpy(op.rlinb, p.rlb, sizeof op.rlinb);
+  int src[kMaxD];
+  for (int a = 0; a < D; a++) {
+    int j = 0;
+    for (int c = 0; c < D; c++)
+      if (p.U[a * D + c] != cplx(0, 0)) op.col[a * D + j++] = (int8_t)c;
+    op.nnz[a] = (int8_t)j;
+    src[a] = j > 0 ? op.col[a * D] : a;
+    op.src[a] = (int8_t)src[a];
+  }
+  const bool mono = p.cls == CLS_MOVE || p.cls == CLS_SIGNED || p.cls == CLS_PHASE;
+  for (int a = 0; a < D; a++)
+    for (int b = 0; b < D; b++) {
+      int8_t fk = FK_GEN;
+      if (mono) {
+        const cplx f = p.U[a * D + src[a]] * std::conj(p.U[b * D + src[b]]);
+        const double fr = snap1(f.real(), kSnapFactor), fi = snap1(f.imag(), kSnapFactor);
+        op.fre[a * D + b] = fr;
+        op.fim[a * D + b] = fi;
+        if (fr == 1.0 && fi == 0.0) fk = FK_ONE;
+        else if (fr == -1.0 && fi == 0.0) fk = FK_NEG;
+        else if (fr == 0.0 && fi == 1.0) fk = FK_PI;
+        else if (fr == 0.0 && fi == -1.0) fk = FK_NI;
+      }
+      op.fk[a * D + b] = fk;
+    }
+
+  // run masks
+  auto run_of = [&](int a, int b) {
+    int r = 0;
+    for (int j = 0; j < h.mhi; j++) {
+      const int x = hi[j];
+      int bit = 0;
+      for (int i = 0; i < K; i++) {
+        if (x == p.q[i]) bit = (a >> i) & 1;
+        if (x == p.q[i] + n) bit = (b >> i) & 1;
+      }
+      r |= bit << j;
+    }
+    return r;
+  };
+  auto row_identity = [&](int a) {
+    for (int c = 0; c < D; c++)
+      if (p.U[a * D + c] != (c == a ? cplx(1, 0) : cplx(0, 0))) return false;
+    return true;
+  };
+  std::vector<char> st(1 << h.mhi, 0), ld(1 << h.mhi, 0);
+  for (int a = 0; a < D; a++)
+    for (int b = 0; b < D; b++) {
+      bool changed;
+      if (p.cls == CLS_RLIN) changed = true;
+      else if (mono) changed = src[a] != a || src[b] != b || op.fk[a * D + b] != FK_ONE;
+      else changed = !(row_identity(a) && row_identity(b));
+      if (changed) st[run_of(a, b)] = 1;
+    }
+  for (int a = 0; a < D; a++)
+    for (int b = 0; b < D; b++) {
+      if (!st[run_of(a, b)]) continue;
+      ld[run_of(a, b)] = 1;
+      if (p.cls == CLS_RLIN) {
+        for (int a2 = 0; a2 < D; a2++)
+          for (int b2 = 0; b2 < D; b2++) ld[run_of(a2, b2)] = 1;
+      } else if (mono) {
+        ld[run_of(src[a], src[b])] = 1;
+      } else {
+        for (int c = 0; c < D; c++) {
+          if (p.U[a * D + c] == cplx(0, 0)) continue;
+          for (int e = 0; e < D; e++)
+            if (p.U[b * D + e] != cplx(0, 0)) ld[run_of(c, e)] = 1;
+        }
+      }
+    }
+  // DENSE and RLIN multiply every entry of a column, structural zeros
+  // included, so every run is loaded: an unloaded run would feed
+  // uninitialised shared memory (possibly NaN, and 0*NaN = NaN) into stored
+  // entries.  MOVE/SIGNED/PHASE/SPARSE read only the sources listed above.
+  if (p.cls == CLS_DENSE || p.cls == CLS_RLIN) std::fill(ld.begin(), ld.end(), 1);
+  int nst = 0, nld = 0;
+  for (int r = 0; r < (1 << h.mhi); r++) {
+    if (st[r]) {
+      h.stmask[r >> 5] |= 1u << (r & 31);
+      nst++;
+    }
+    if (ld[r]) {
+      h.ldmask[r >> 5] |= 1u << (r & 31);
+      nld++;
+    }
+  }
+  const uint64_t runlen = 1ull << L;
+  const uint64_t entries = (uint64_t)(nst + nld) * runlen * h.ntiles;
+  if (ntiles_out) *ntiles_out = h.ntiles;
+  if (tile_out) *tile_out = (1 << g) * D * D;
+  if (feat) {
+    feat->K = K;
+    feat->cls = p.cls;
+    feat->nnz = p.nnz;
+    feat->n = n;
+    int lo = -1, hmin = nb;
+    for (int x : P) {
+      if (x < L) lo = std::max(lo, x);
+      else hmin = std::min(hmin, x);
+    }
+    feat->max_lo_bit = lo;
+    feat->min_hi_bit = hmin;
+    const double tot = (double)(1 << h.mhi);
+    feat->ld_frac = nld / tot;
+    feat->st_frac = nst / tot;
+  }
+  return entries;
+}
+
+}  // namespace
+
+uint64_t build_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries) {
+  switch (p.K) {
+    case 1: return build_k<1>(p, n, static_cast<PassDesc<1>*>(out), f, ntiles, tile_entries);
+    case 2: return build_k<2>(p, n, static_cast<PassDesc<2>*>(out), f, ntiles, tile_entries);
+    case 3: return build_k<3>(p, n, static_cast<PassDesc<3>*>(out), f, ntiles, tile_entries);
+    default: return build_k<4>(p, n, static_cast<PassDesc<4>*>(out), f, ntiles, tile_entries);
+  }
+}
+
+}  // namespace dmg

@@ -1,0 +1,51 @@
+// plan.h -- from basic gates to device passes.
+#pragma once
+#include <stdint.h>
+
+#include <vector>
+
+#include "gates.h"
+#include "pass.h"
+
+namespace dmg {
+
+// A pass before it is written to the device: a K-qubit operator on qubits
+// q[0..K-1] (sub-index bit i <-> qubit q[i]) and its arithmetic class.
+struct PassSpec {
+  int K = 0;
+  int q[kMaxK] = {0, 0, 0, 0};
+  cplx U[kMaxD * kMaxD];       // row-major D x D
+  bool rlin = false;
+  double rl[16], rlb[16];
+  int cls = CLS_DENSE;
+  int nbasic = 0;              // basic gates this pass replaces
+  int nnz = 0;                 // nonzeros of U after snapping
+};
+
+// Cost-model features of one pass (also recorded with its measured time).
+struct PassFeatures {
+  int K, cls, nnz;
+  int max_lo_bit;   // highest target bit below L (-1 if none)
+  int min_hi_bit;   // lowest target bit at or above L (2n if none)
+  int n;
+  double ld_frac, st_frac;  // fraction of the state read / written
+};
+
+// Fusion planners.  Both keep program order on every qubit and only reorder
+// gates that act on disjoint qubits.
+//   greedy: grow each pass with the earliest ready gate that keeps the width <= maxk
+//   (prefer gates inside the current qubit set), the fixed-width planner.
+std::vector<PassSpec> plan_plain(const std::vector<Basic>& basics);
+std::vector<PassSpec> plan_greedy(const std::vector<Basic>& basics, int maxk);
+
+// Snap near-exact entries, detect the arithmetic class.
+void classify(PassSpec& p, bool fused);
+
+// Size in bytes of the device descriptor of a width-K pass.
+size_t desc_size(int K);
+// Write the descriptor of pass p for an n-qubit state into out (desc_size bytes).
+// Returns the algorithmic bytes per entry-size unit moved by the pass
+// (entries read + entries written); features are filled when f != nullptr.
+uint64_t build_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries);
+
+}  // namespace dmg

@@ -1,0 +1,343 @@
+"""Python binding of the GB300 density-matrix engine's C ABI (include/dmsim_gb300.h).
+
+Every call goes to ``libdmsim_gb300.so`` (hand-written sm_103a kernels behind a
+C ABI).  There is no fallback: if the library is missing, importing this
+module raises ``ImportError`` with the build command.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.normpath(os.path.join(_HERE, "..", "lib", "libdmsim_gb300.so"))
+
+OK, ERR_ARG, ERR_STATE, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_UNSUPPORTED = range(7)
+OPT_MODE, OPT_PRECISION, OPT_MAX_K, OPT_PLANNER, OPT_RECORD, OPT_SEED, OPT_GRAPH, OPT_VERBOSE = range(1, 9)
+
+OP_NAMES = ["U3", "U2", "U1", "CX", "ID", "X", "Y", "Z", "H", "S",
+            "SDG", "T", "TDG", "RX", "RY", "RZ", "CZ", "CY", "SWAP", "CH",
+            "CCX", "CSWAP", "CRX", "CRY", "CRZ", "CU1", "CU3", "RXX", "RZZ", "RCCX",
+            "RC3X", "C3X", "C3SQRTX", "C4X", "R", "SRN", "W", "RYY"]
+OP = {n: i for i, n in enumerate(OP_NAMES)}
+
+CLASS_NAMES = ["MOVE", "SIGNED", "PHASE", "DENSE", "SPARSE", "RLIN"]
+
+
+class DMSimError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"dmsim error {status}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib():
+    """The loaded engine library (ctypes), with argument types declared."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with "
+                          f"`python -c 'import __graft_entry__ as g; g.build()'` at the repository root")
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.POINTER
+    H = ctypes.c_void_p
+    d, u32, u64, i64 = ctypes.c_double, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int64
+    sig = {
+        "dmsim_create": [u32, u32, P(H)],
+        "dmsim_destroy": [H],
+        "dmsim_set_option": [H, ctypes.c_int, i64],
+        "dmsim_get_option": [H, ctypes.c_int, P(i64)],
+        "dmsim_append": [H, ctypes.c_int, P(u32), d, d, d],
+        "dmsim_append_c1": [H, u32, P(d)],
+        "dmsim_append_c2": [H, u32, u32, P(d)],
+        "dmsim_upload": [H],
+        "dmsim_run": [H],
+        "dmsim_clear_circuit": [H],
+        "dmsim_reset": [H],
+        "dmsim_reset_dm": [H],
+        "dmsim_measure": [H, u32, P(d), P(u64)],
+        "dmsim_get_dm": [H, P(d), P(d)],
+        "dmsim_set_dm": [H, P(d), P(d)],
+        "dmsim_get_diag": [H, P(d)],
+        "dmsim_dump": [H, ctypes.c_char_p, ctypes.c_size_t, P(ctypes.c_size_t)],
+        "dmsim_n_qubits": [H, P(u32)],
+        "dmsim_n_gates": [H, P(u32)],
+        "dmsim_plan_stats": [H, P(u32), P(u32)],
+        "dmsim_last_timings": [H, P(d)],
+        "dmsim_pass_records": [H, P(d), u32, P(u32)],
+        "dmsim_pure_metrics": [H, P(d), P(d), P(d)],
+        "dmsim_device_state": [H, P(ctypes.c_void_p), P(ctypes.c_void_p)],
+        "dmsim_compare_states": [H, H, P(d)],
+        "dmsim_alloc_host": [ctypes.c_size_t, P(ctypes.c_void_p)],
+        "dmsim_free_host": [ctypes.c_void_p],
+        "dmsim_plan_inspect": [u32, P(ctypes.c_int32), P(u32), P(d), P(d), u32, ctypes.c_int, ctypes.c_int,
+                               ctypes.c_int, P(d), u32, P(u32)],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = ctypes.c_int
+    L.dmsim_last_error.argtypes = [H]
+    L.dmsim_last_error.restype = ctypes.c_char_p
+    L.dmsim_status_string.argtypes = [ctypes.c_int]
+    L.dmsim_status_string.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Simulation:
+    """One density matrix on the current CUDA device.
+
+    ``precision`` is "fp64" or "c64"; ``mode`` is "plain" (one pass per basic
+    gate, the reference's method) or "fused"; ``planner`` is "greedy" or
+    "learned" (fused mode only).
+    """
+
+    def __init__(self, n_qubits, n_gpus=1, precision="fp64", mode="plain", max_k=4, planner="greedy",
+                 graph=True):
+        self._h = ctypes.c_void_p()
+        self.n = int(n_qubits)
+        st = lib().dmsim_create(self.n, int(n_gpus), ctypes.byref(self._h))
+        if st != OK:
+            raise DMSimError(st, lib().dmsim_status_string(st).decode())
+        try:
+            self.set_option(OPT_PRECISION, 1 if precision == "c64" else 0)
+            self.set_option(OPT_MODE, 1 if mode == "fused" else 0)
+            self.set_option(OPT_MAX_K, int(max_k))
+            self.set_option(OPT_PLANNER, 1 if planner == "learned" else 0)
+            self.set_option(OPT_GRAPH, 1 if graph else 0)
+        except Exception:
+            self.close()
+            raise
+
+    # -- plumbing
+    def _check(self, st):
+        if st != OK:
+            raise DMSimError(st, lib().dmsim_last_error(self._h).decode())
+
+    def close(self):
+        if self._h:
+            lib().dmsim_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_option(self, key, value):
+        self._check(lib().dmsim_set_option(self._h, key, int(value)))
+
+    def get_option(self, key):
+        v = ctypes.c_int64()
+        self._check(lib().dmsim_get_option(self._h, key, ctypes.byref(v)))
+        return v.value
+
+    # -- circuit
+    def append(self, op, qubits, theta=0.0, phi=0.0, lam=0.0):
+        q = list(qubits) + [0] * (5 - len(qubits))
+        self._check(lib().dmsim_append(self._h, int(op), (ctypes.c_uint32 * 5)(*q), theta, phi, lam))
+
+    def append_c1(self, q, m):
+        m = np.asarray(m, dtype=np.complex128).reshape(4)
+        flat = np.empty(8)
+        flat[0::2], flat[1::2] = m.real, m.imag
+        self._check(lib().dmsim_append_c1(self._h, int(q), _dp(flat)))
+
+    def append_c2(self, q1, q2, m):
+        m = np.asarray(m, dtype=np.complex128).reshape(16)
+        flat = np.empty(32)
+        flat[0::2], flat[1::2] = m.real, m.imag
+        self._check(lib().dmsim_append_c2(self._h, int(q1), int(q2), _dp(flat)))
+
+    def extend(self, circuit):
+        for g in circuit:
+            self.append(g[0], g[1], g[2], g[3], g[4])
+
+    def upload(self):
+        self._check(lib().dmsim_upload(self._h))
+
+    def run(self):
+        self._check(lib().dmsim_run(self._h))
+
+    def clear_circuit(self):
+        self._check(lib().dmsim_clear_circuit(self._h))
+
+    def reset(self):
+        self._check(lib().dmsim_reset(self._h))
+
+    def reset_dm(self):
+        self._check(lib().dmsim_reset_dm(self._h))
+
+    # -- results
+    def measure(self, rep=10, uniforms=None):
+        out = np.zeros(rep, dtype=np.uint64)
+        up = None
+        if uniforms is not None:
+            u = np.ascontiguousarray(uniforms, dtype=np.float64)
+            assert len(u) == rep
+            up = _dp(u)
+        self._check(lib().dmsim_measure(self._h, rep, up, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))))
+        return [int(x) for x in out]
+
+    def get_dm(self):
+        N = 1 << (2 * self.n)
+        re, im = np.empty(N), np.empty(N)
+        self._check(lib().dmsim_get_dm(self._h, _dp(re), _dp(im)))
+        return re, im
+
+    def set_dm(self, re, im):
+        re = np.ascontiguousarray(re, dtype=np.float64)
+        im = np.ascontiguousarray(im, dtype=np.float64)
+        assert re.size == 1 << (2 * self.n) and im.size == re.size
+        self._check(lib().dmsim_set_dm(self._h, _dp(re), _dp(im)))
+
+    def get_diag(self):
+        d = np.empty(1 << self.n)
+        self._check(lib().dmsim_get_diag(self._h, _dp(d)))
+        return d
+
+    def rho(self):
+        """rho as a complex (2^n x 2^n) matrix: rho[r][c] = A[c*2^n + r]."""
+        re, im = self.get_dm()
+        d = 1 << self.n
+        return (re.reshape(d, d) + 1j * im.reshape(d, d)).T
+
+    def dump(self):
+        need = ctypes.c_size_t()
+        self._check(lib().dmsim_dump(self._h, None, 0, ctypes.byref(need)))
+        buf = ctypes.create_string_buffer(need.value)
+        self._check(lib().dmsim_dump(self._h, buf, need.value, None))
+        return buf.value.decode()
+
+    def n_gates(self):
+        v = ctypes.c_uint32()
+        self._check(lib().dmsim_n_gates(self._h, ctypes.byref(v)))
+        return v.value
+
+    def plan_stats(self):
+        a, b = ctypes.c_uint32(), ctypes.c_uint32()
+        self._check(lib().dmsim_plan_stats(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def last_timings(self):
+        o = np.zeros(3)
+        self._check(lib().dmsim_last_timings(self._h, _dp(o)))
+        return {"ms": o[0], "passes": int(o[1]), "bytes": o[2]}
+
+    def pass_records(self):
+        cnt = ctypes.c_uint32()
+        self._check(lib().dmsim_pass_records(self._h, None, 0, ctypes.byref(cnt)))
+        out = np.zeros((cnt.value, 8))
+        if cnt.value:
+            self._check(lib().dmsim_pass_records(self._h, _dp(out), cnt.value, ctypes.byref(cnt)))
+        return out
+
+    def pure_metrics(self, psi):
+        psi = np.asarray(psi, dtype=np.complex128)
+        pr, pi = np.ascontiguousarray(psi.real), np.ascontiguousarray(psi.imag)
+        o = np.zeros(4)
+        self._check(lib().dmsim_pure_metrics(self._h, _dp(pr), _dp(pi), _dp(o)))
+        return {"fidelity": o[0], "trace": o[1], "max_abs_err": o[2], "frob_err": o[3]}
+
+    def compare(self, other):
+        """max |A - B| and ||A - B||_F between this state and another, on the device."""
+        o = np.zeros(2)
+        self._check(lib().dmsim_compare_states(self._h, other._h, _dp(o)))
+        return {"max_abs_err": o[0], "frob_err": o[1]}
+
+    def get_dm_into(self, re, im):
+        """Copy rho into caller-provided float64 buffers (e.g. PinnedBuffer arrays)."""
+        self._check(lib().dmsim_get_dm(self._h, _dp(re), _dp(im)))
+
+    def device_state(self):
+        re, im = ctypes.c_void_p(), ctypes.c_void_p()
+        self._check(lib().dmsim_device_state(self._h, ctypes.byref(re), ctypes.byref(im)))
+        return re.value, im.value
+
+
+PASS_REC = 520
+
+
+def plan_inspect(n, circuit, mode="fused", max_k=4, planner="greedy"):
+    """Plan a circuit on the host only (no GPU): list of passes with their
+    width, class, qubits and operator, as dmsim_upload would build them.
+
+    ``circuit`` holds (op, qubits, theta, phi, lam[, matrix]) tuples."""
+    m = len(circuit)
+    ops = np.zeros(max(m, 1), dtype=np.int32)
+    qs = np.zeros(5 * max(m, 1), dtype=np.uint32)
+    ps = np.zeros(3 * max(m, 1))
+    mats = np.zeros(32 * max(m, 1))
+    for i, g in enumerate(circuit):
+        ops[i] = g[0]
+        for k, q in enumerate(g[1]):
+            qs[5 * i + k] = q
+        ps[3 * i:3 * i + 3] = g[2], g[3], g[4]
+        if len(g) > 5 and g[5] is not None:
+            mm = np.asarray(g[5], dtype=np.complex128).reshape(-1)
+            mats[32 * i:32 * i + 2 * mm.size:2] = mm.real
+            mats[32 * i + 1:32 * i + 2 * mm.size:2] = mm.imag
+    L = lib()
+    P = ctypes.POINTER
+    cnt = ctypes.c_uint32()
+    args = (n, ops.ctypes.data_as(P(ctypes.c_int32)), qs.ctypes.data_as(P(ctypes.c_uint32)), _dp(ps), _dp(mats), m,
+            1 if mode == "fused" else 0, int(max_k), 1 if planner == "learned" else 0)
+    st = L.dmsim_plan_inspect(*args, None, 0, ctypes.byref(cnt))
+    if st != OK:
+        raise DMSimError(st, L.dmsim_status_string(st).decode())
+    out = np.zeros((max(cnt.value, 1), PASS_REC))
+    st = L.dmsim_plan_inspect(*args, _dp(out), cnt.value, ctypes.byref(cnt))
+    if st != OK:
+        raise DMSimError(st, L.dmsim_status_string(st).decode())
+    passes = []
+    for r in out[:cnt.value]:
+        K = int(r[0])
+        D = 1 << K
+        rec = {"K": K, "cls": CLASS_NAMES[int(r[1])], "nbasic": int(r[2]), "nnz": int(r[3]),
+               "qubits": [int(x) for x in r[4:4 + K]]}
+        if rec["cls"] == "RLIN":
+            rec["rl"] = r[8:24].reshape(4, 4).copy()
+            rec["rlb"] = r[24:40].reshape(4, 4).copy()
+        else:
+            u = r[8:8 + 2 * D * D]
+            rec["U"] = (u[0::2] + 1j * u[1::2]).reshape(D, D)
+        passes.append(rec)
+    return passes
+
+
+class PinnedBuffer:
+    """A page-locked host float64 array (cudaHostAlloc) for fast copies."""
+
+    def __init__(self, count):
+        self._p = ctypes.c_void_p()
+        st = lib().dmsim_alloc_host(int(count) * 8, ctypes.byref(self._p))
+        if st != OK:
+            raise DMSimError(st, "pinned host allocation failed")
+        self.array = np.ctypeslib.as_array(ctypes.cast(self._p, ctypes.POINTER(ctypes.c_double)), shape=(int(count),))
+
+    def close(self):
+        if self._p:
+            self.array = None
+            lib().dmsim_free_host(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

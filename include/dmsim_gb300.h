@@ -1,0 +1,134 @@
+/*
+ * dmsim_gb300.h -- C ABI of the GB300 density-matrix gate engine.
+ *
+ * Plain pointers and sizes only; every call returns a status code (0 = ok)
+ * and never exits the process.  One handle owns one density matrix on the
+ * current CUDA device and one CUDA stream; calls on one handle must be
+ * serialised by the caller (the reference object is not thread-safe either).
+ *
+ * Each entry point replaces a member of DM-Sim's Simulation class
+ * (src/dmsim_nvgpu_omp.cuh in pnnl/DM-Sim); the citation is given per entry.
+ */
+#ifndef DMSIM_GB300_H
+#define DMSIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct dmsim_sim* dmsim_handle;
+
+enum dmsim_status {
+  DMSIM_OK = 0,
+  DMSIM_ERR_ARG = 1,          /* bad qubit index, unknown gate id, null pointer, bad size */
+  DMSIM_ERR_STATE = 2,        /* call out of order (upload twice, run before upload) */
+  DMSIM_ERR_OOM = 3,          /* device or pinned host allocation failed */
+  DMSIM_ERR_CUDA = 4,         /* CUDA runtime error (message in dmsim_last_error) */
+  DMSIM_ERR_TIMEOUT = 5,      /* a bounded device wait ran out */
+  DMSIM_ERR_UNSUPPORTED = 6   /* e.g. n_gpus != 1: this engine is single-GPU */
+};
+
+/* Runtime options (dmsim_set_option).  Defaults in brackets. */
+enum dmsim_option {
+  DMSIM_OPT_MODE = 1,       /* 0 = plain gate-by-gate [0], 1 = fused */
+  DMSIM_OPT_PRECISION = 2,  /* 0 = FP64 [0], 1 = complex64 (FP32 passes, FP64 reductions); set before the first append */
+  DMSIM_OPT_MAX_K = 3,      /* widest fused operator, 1..4 [4] */
+  DMSIM_OPT_PLANNER = 4,    /* 0 = greedy fixed width [0], 1 = learned cost model */
+  DMSIM_OPT_RECORD = 5,     /* 1 = time every pass of the next runs (no graph) [0] */
+  DMSIM_OPT_SEED = 6,       /* seed of measure() without uniforms; -1 = time(0) like the reference [-1] */
+  DMSIM_OPT_GRAPH = 7,      /* 1 = replay uploaded circuits from a captured CUDA graph [1] */
+  DMSIM_OPT_VERBOSE = 8     /* 1 = print the reference's per-run timing banner [0] */
+};
+
+/* Gate ids: the order of enum OP, src/dmsim_nvgpu_omp.cuh:42-48 (ABI). */
+enum dmsim_op {
+  DMSIM_U3 = 0, DMSIM_U2, DMSIM_U1, DMSIM_CX, DMSIM_ID, DMSIM_X, DMSIM_Y, DMSIM_Z, DMSIM_H, DMSIM_S,
+  DMSIM_SDG, DMSIM_T, DMSIM_TDG, DMSIM_RX, DMSIM_RY, DMSIM_RZ, DMSIM_CZ, DMSIM_CY, DMSIM_SWAP, DMSIM_CH,
+  DMSIM_CCX, DMSIM_CSWAP, DMSIM_CRX, DMSIM_CRY, DMSIM_CRZ, DMSIM_CU1, DMSIM_CU3, DMSIM_RXX, DMSIM_RZZ, DMSIM_RCCX,
+  DMSIM_RC3X, DMSIM_C3X, DMSIM_C3SQRTX, DMSIM_C4X, DMSIM_R, DMSIM_SRN, DMSIM_W, DMSIM_RYY,
+  DMSIM_N_OPS
+};
+
+/* Simulation(n_qubits, n_gpus) -- src/dmsim_nvgpu_omp.cuh:196-271.  Allocates
+ * rho = |0..0><0..0| on the current device.  n_gpus must be 1. */
+int dmsim_create(uint32_t n_qubits, uint32_t n_gpus, dmsim_handle* out);
+/* ~Simulation() -- :273-301 */
+int dmsim_destroy(dmsim_handle h);
+int dmsim_set_option(dmsim_handle h, int key, int64_t value);
+int dmsim_get_option(dmsim_handle h, int key, int64_t* value);
+
+/* append(Gate*) -- :331-344, with the Gate fields of :99-191 (op, qb0..qb4,
+ * theta, phi, lambda).  Qubits must be < n_qubits and distinct where the gate
+ * uses them. */
+int dmsim_append(dmsim_handle h, int op, const uint32_t qb[5], double theta, double phi, double lambda);
+/* Arbitrary 1-qubit gate (README "C1"; element formulas of C1_GATE :1004-1025).
+ * m = 2x2 complex, row-major, re/im interleaved (8 doubles). */
+int dmsim_append_c1(dmsim_handle h, uint32_t q, const double m[8]);
+/* Arbitrary 2-qubit gate (README "C2"; C2_GATE :1028-1122): m = 4x4 complex,
+ * row-major, re/im interleaved (32 doubles), basis index 2*bit(q1) + bit(q2). */
+int dmsim_append_c2(dmsim_handle h, uint32_t q1, uint32_t q2, const double m[32]);
+/* upload() -- :345-377.  Plans the passes and copies them to the device once. */
+int dmsim_upload(dmsim_handle h);
+/* sim() -- :390-494, without the copy of rho to the host (dmsim_get_dm). */
+int dmsim_run(dmsim_handle h);
+/* clear_circuit() -- :496-520.  rho is kept (chained circuits). */
+int dmsim_clear_circuit(dmsim_handle h);
+/* reset() -- :303-307: clear_circuit + reset_dm */
+int dmsim_reset(dmsim_handle h);
+/* reset_dm() -- :308-329: rho = |0..0><0..0| */
+int dmsim_reset_dm(dmsim_handle h);
+/* measure(rep) -- :521-549.  uniforms[rep] replace rand()/RAND_MAX when not
+ * NULL; otherwise srand(seed option) + rand() as the reference.  out[rep].
+ * The probability prefix is the reference's sequential FP64 sum. */
+int dmsim_measure(dmsim_handle h, uint32_t rep, const double* uniforms, uint64_t* out);
+/* dm_real_res / dm_imag_res -- :456-459, :790-791: re[i*dim+j] + i*im[i*dim+j]
+ * = rho[j][i].  Buffers hold 4^n doubles each. */
+int dmsim_get_dm(dmsim_handle h, double* re, double* im);
+/* Load rho from host buffers in the same layout. */
+int dmsim_set_dm(dmsim_handle h, const double* re, const double* im);
+/* diag[i] = Re rho[i][i], 2^n doubles */
+int dmsim_get_diag(dmsim_handle h, double* diag);
+/* dump() -- :379-387: one line per gate; returns the length needed (incl. NUL). */
+int dmsim_dump(dmsim_handle h, char* buf, size_t len, size_t* needed);
+int dmsim_n_qubits(dmsim_handle h, uint32_t* n);
+int dmsim_n_gates(dmsim_handle h, uint32_t* n);
+/* Passes of the uploaded plan and basic gates they replace. */
+int dmsim_plan_stats(dmsim_handle h, uint32_t* n_passes, uint32_t* n_basic);
+/* Timing of the last run: out[0] = ms, out[1] = passes, out[2] = bytes moved (algorithmic) */
+int dmsim_last_timings(dmsim_handle h, double out[3]);
+/* Per-pass records of the last recorded run (DMSIM_OPT_RECORD): for each pass
+ * 8 doubles {K, class, nnz, max_lo_bit, min_hi_bit, n, ms, bytes}. Returns count. */
+int dmsim_pass_records(dmsim_handle h, double* out, uint32_t cap, uint32_t* count);
+/* Compare rho with a pure state psi (2^n complex, FP64) on the device:
+ * out[0] = fidelity <psi|rho|psi>, out[1] = trace, out[2] = max |rho - psi psi^+|,
+ * out[3] = ||rho - psi psi^+||_F. */
+int dmsim_pure_metrics(dmsim_handle h, const double* psi_re, const double* psi_im, double out[4]);
+/* Compare two states of the same size and precision on the device:
+ * out[0] = max |A - B| over entries, out[1] = ||A - B||_F. */
+int dmsim_compare_states(dmsim_handle a, dmsim_handle b, double out[2]);
+/* Page-locked host buffers for fast dmsim_get_dm / dmsim_set_dm copies. */
+int dmsim_alloc_host(size_t bytes, void** out);
+int dmsim_free_host(void* p);
+/* Host-only planning (no GPU needed): decompose and plan a circuit exactly as
+ * dmsim_upload would and return, per pass, DMSIM_PASS_REC doubles:
+ * {K, class, n_basic, nnz, q0, q1, q2, q3} followed by the 16x16 complex
+ * operator (re/im interleaved, row stride 2^K; for the real-linear class the
+ * ket map then the bra map, 16 doubles each).  ops[i], qubits[5*i..], params
+ * [3*i..] = theta, phi, lambda; mats[32*i..] holds C1/C2 matrices (may be NULL
+ * when there are none).  Returns the pass count in *npasses. */
+#define DMSIM_PASS_REC 520
+int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qubits, const double* params,
+                       const double* mats, uint32_t ngates, int mode, int max_k, int planner,
+                       double* out, uint32_t cap, uint32_t* npasses);
+/* Device pointers of rho (for in-HBM benchmarks and interop) */
+int dmsim_device_state(dmsim_handle h, void** re, void** im);
+const char* dmsim_last_error(dmsim_handle h);
+const char* dmsim_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

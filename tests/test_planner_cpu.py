@@ -1,0 +1,125 @@
+"""Host-side planning, checked on the CPU (no GPU): the passes that upload()
+would run, applied in numpy as U (x) conj(U) superoperators (or the real-linear
+map for SRN), reproduce the oracle's density matrix; fused passes respect the
+width limit and program order on every qubit."""
+import numpy as np
+import pytest
+
+import dmsim_workloads as W
+
+
+def apply_pass_dm(rho, n, p):
+    """rho[r][c]; apply the pass to ket (rows) and bra (columns)."""
+    K, qs = p["K"], p["qubits"]
+    d = 1 << n
+    t = rho.reshape([2] * (2 * n))  # axes: row bits (n-1 .. 0), then col bits (n-1 .. 0)
+    row_ax = [n - 1 - q for q in qs]      # axis of row bit q
+    col_ax = [2 * n - 1 - q for q in qs]  # axis of col bit q
+    if p["cls"] == "RLIN":
+        # real-linear 2x2 map: on (re0, im0, re1, im1) of the row pair, then the bra map on the column pair
+        M, Mb = p["rl"], p["rlb"]
+
+        def rl(x, ax, M):
+            x = np.moveaxis(x, ax, 0)
+            v = np.stack([x[0].real, x[0].imag, x[1].real, x[1].imag])
+            o = np.tensordot(M, v, axes=1)
+            y = np.stack([o[0] + 1j * o[1], o[2] + 1j * o[3]])
+            return np.moveaxis(y, 0, ax)
+
+        t = rl(t, row_ax[0], M)
+        t = rl(t, col_ax[0], Mb)
+        return t.reshape(d, d)
+    U = p["U"]
+    # U index bit i <-> qubit qs[i]; as a tensor with axes (bit K-1 .. bit 0)
+    Ut = U.reshape([2] * (2 * K))
+    out_axes = list(range(K))
+    in_axes = list(range(K, 2 * K))
+    # contract ket
+    ax_row = [row_ax[K - 1 - i] for i in range(K)]
+    t = np.tensordot(Ut, t, axes=(in_axes, ax_row))
+    t = np.moveaxis(t, out_axes, ax_row)
+    ax_col = [col_ax[K - 1 - i] for i in range(K)]
+    t = np.tensordot(Ut.conj(), t, axes=(in_axes, ax_col))
+    t = np.moveaxis(t, out_axes, ax_col)
+    return t.reshape(d, d)
+
+
+def run_plan(n, circ, mode, max_k, engine):
+    passes = engine.plan_inspect(n, circ, mode=mode, max_k=max_k)
+    d = 1 << n
+    rho = np.zeros((d, d), complex)
+    rho[0, 0] = 1
+    for p in passes:
+        rho = apply_pass_dm(rho, n, p)
+    return rho, passes
+
+
+@pytest.mark.parametrize("mode,max_k", [("plain", 4), ("fused", 1), ("fused", 2), ("fused", 3), ("fused", 4)])
+@pytest.mark.parametrize("seed", [0, 1])
+def test_plan_reproduces_oracle(engine, oracle, mode, max_k, seed):
+    n = 5
+    ops = [o for o in range(38) if o != W.OP["SRN"]]
+    circ = W.random_circuit(n, 50, ops=ops, seed=200 + seed)
+    rho, passes = run_plan(n, circ, mode, max_k, engine)
+    re, im = oracle.dm_sim(n, circ)
+    ref = oracle.rho_from_result(n, re, im)
+    tol = 1e-12 if mode == "plain" else 1e-10
+    assert np.abs(rho - ref).max() < tol
+    assert all(p["K"] <= (2 if mode == "plain" else max(max_k, 2)) for p in passes)
+    nb = sum(oracle.basic_count(g) for g in circ)
+    assert sum(p["nbasic"] for p in passes) == nb - sum(1 for g in circ if g[0] == W.OP["ID"])
+
+
+def test_plain_classes(engine):
+    """Each basic gate lands in the class its structure allows."""
+    n = 3
+    cases = {"X": "MOVE", "CX": "MOVE", "Y": "SIGNED", "Z": "SIGNED", "S": "SIGNED", "SDG": "SIGNED",
+             "T": "PHASE", "TDG": "PHASE", "U1": "PHASE", "H": "DENSE", "U3": "DENSE", "SRN": "RLIN"}
+    for name, cls in cases.items():
+        op = W.OP[name]
+        qs = (0, 1) if W.ARITY[op] == 2 else (1,)
+        p = engine.plan_inspect(n, [(op, qs, 0.3, 0.2, 0.1)], mode="plain")
+        assert [x["cls"] for x in p] == [cls], name
+
+
+def test_fused_toffoli_is_pure_data_movement(engine):
+    """CCX's 15 basic gates fuse into one K=3 pass whose operator is Toffoli
+    exactly (structural zeros/ones restored), so the pass needs no arithmetic."""
+    p = engine.plan_inspect(4, [(W.OP["CCX"], (0, 1, 2), 0, 0, 0)], mode="fused", max_k=3)
+    assert len(p) == 1 and p[0]["K"] == 3 and p[0]["nbasic"] == 15
+    assert p[0]["cls"] in ("MOVE", "SIGNED", "PHASE")
+
+
+def test_fusion_keeps_program_order(engine, oracle):
+    """Non-commuting gates on shared qubits in a long chain; fused result must
+    equal the sequential one for every width."""
+    n = 4
+    ops = [W.OP[x] for x in ("H", "CX", "T", "U3", "CZ", "RX", "CU1", "SWAP")]
+    circ = W.random_circuit(n, 120, ops=ops, seed=9)
+    re, im = oracle.dm_sim(n, circ)
+    ref = oracle.rho_from_result(n, re, im)
+    for k in (1, 2, 3, 4):
+        rho, _ = run_plan(n, circ, "fused", k, engine)
+        assert np.abs(rho - ref).max() < 1e-10, k
+
+
+def test_c1_c2_additions(engine, oracle):
+    rng = np.random.default_rng(3)
+    def rand_u(d):
+        q, _ = np.linalg.qr(rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d)))
+        return q
+    n = 4
+    circ = [(64, (1,), 0, 0, 0, rand_u(2)), (W.OP["H"], (2,), 0, 0, 0), (65, (3, 0), 0, 0, 0, rand_u(4)),
+            (65, (0, 2), 0, 0, 0, rand_u(4)), (64, (3,), 0, 0, 0, rand_u(2))]
+    re, im = oracle.dm_sim(n, circ)
+    ref = oracle.rho_from_result(n, re, im)
+    for mode, k in (("plain", 4), ("fused", 2), ("fused", 4)):
+        rho, _ = run_plan(n, circ, mode, k, engine)
+        assert np.abs(rho - ref).max() < 1e-12, (mode, k)
+
+
+def test_bad_inputs_rejected_on_host(engine):
+    with pytest.raises(engine.DMSimError):
+        engine.plan_inspect(3, [(W.OP["CX"], (0, 5), 0, 0, 0)])
+    with pytest.raises(engine.DMSimError):
+        engine.plan_inspect(3, [(99, (0,), 0, 0, 0)])
