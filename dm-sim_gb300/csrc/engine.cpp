@@ -128,6 +128,12 @@ void check_qubits(const dmsim_sim* s, const GateRec& g) {
 void enqueue_passes(dmsim_sim* s, bool timed) {
   for (size_t i = 0; i < s->passes.size(); i++) {
     PassInfo& p = s->passes[i];
+    if (p.transpose) {
+      if (timed) DM_CUDA(cudaEventRecord(p.ev0, s->stream));
+      DM_CUDA(launch_conj_transpose(s->d_re, s->d_im, (int)s->n, s->fp32, p.grid, s->stream));
+      if (timed) DM_CUDA(cudaEventRecord(p.ev1, s->stream));
+      continue;
+    }
     LaunchArgs a;
     a.re = s->d_re;
     a.im = s->d_im;
@@ -143,28 +149,45 @@ void enqueue_passes(dmsim_sim* s, bool timed) {
   }
 }
 
+// Plain: one pass per basic gate.  Fused: the greedy (fixed-width) or the
+// learned planner.  A circuit holding a real-linear gate (SRN) runs in the
+// reference's own order in either mode, the only order that reproduces it.
+std::vector<PassSpec> make_plan(dmsim_sim* s, const std::vector<Basic>& basics) {
+  bool has_rlin = false;
+  for (const Basic& b : basics) has_rlin |= b.kind == BK_RLIN;
+  if (has_rlin) return plan_reference_order(basics);
+  if (s->mode == 0) return plan_plain(basics);
+  if (s->planner == 1) throw DmError{DMSIM_ERR_UNSUPPORTED, "the learned planner is not available in this build"};
+  return plan_greedy(basics, s->maxk);
+}
+
 void upload(dmsim_sim* s) {
   if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "upload() called twice without clear_circuit() (:347-350)"};
   ensure_state(s);
   std::vector<Basic> basics;
   for (const GateRec& g : s->circuit) decompose(g, basics);
   s->n_basic = (uint32_t)basics.size();
-  std::vector<PassSpec> specs;
-  if (s->mode == 0) specs = plan_plain(basics);
-  else if (s->planner == 1) throw DmError{DMSIM_ERR_UNSUPPORTED, "the learned planner is not available in this build"};
-  else specs = plan_greedy(basics, s->maxk);
+  std::vector<PassSpec> specs = make_plan(s, basics);
   // descriptors, 256-byte aligned, one host blob, one copy
   std::vector<size_t> offs;
   size_t total = 0;
   for (const PassSpec& p : specs) {
     offs.push_back(total);
-    total += (desc_size(p.K) + 255) & ~(size_t)255;
+    if (!p.transpose) total += (desc_size(p.K) + 255) & ~(size_t)255;
   }
   std::vector<unsigned char> blob(std::max<size_t>(total, 256));
   s->passes.clear();
   for (size_t i = 0; i < specs.size(); i++) {
     PassInfo pi;
     std::memset(&pi, 0, sizeof pi);
+    if (specs[i].transpose) {
+      pi.transpose = true;
+      pi.K = 0;
+      pi.grid = (unsigned)s->sms * 8;
+      pi.bytes = 2.0 * 2.0 * (double)s->N * (double)esize(s);
+      s->passes.push_back(pi);
+      continue;
+    }
     uint64_t ntiles = 0;
     int tile = 0;
     const uint64_t entries = build_desc(specs[i], (int)s->n, blob.data() + offs[i], &pi.feat, &ntiles, &tile);
@@ -684,8 +707,11 @@ int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qu
         if (g.qb[k] >= n_qubits) return DMSIM_ERR_ARG;
       decompose(g, basics);
     }
+    bool has_rlin = false;
+    for (const Basic& b : basics) has_rlin |= b.kind == BK_RLIN;
     std::vector<PassSpec> specs;
-    if (mode == 0) specs = plan_plain(basics);
+    if (has_rlin) specs = plan_reference_order(basics);
+    else if (mode == 0) specs = plan_plain(basics);
     else if (planner == 1) return DMSIM_ERR_UNSUPPORTED;
     else specs = plan_greedy(basics, max_k);
     if (npasses) *npasses = (uint32_t)specs.size();
@@ -699,14 +725,19 @@ int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qu
         o[2] = p.nbasic;
         o[3] = p.nnz;
         for (int k = 0; k < p.K; k++) o[4 + k] = p.q[k];
+        o[8] = p.ket_only ? 1 : 0;
+        o[9] = p.transpose ? 1 : 0;
+        if (p.transpose) continue;
         if (p.rlin) {
-          std::memcpy(o + 8, p.rl, 16 * sizeof(double));
-          std::memcpy(o + 24, p.rlb, 16 * sizeof(double));
+          std::memcpy(o + 16, p.rl, 16 * sizeof(double));
+          std::memcpy(o + 528, p.rlb, 16 * sizeof(double));
         } else {
           const int D = 1 << p.K;
           for (int j = 0; j < D * D; j++) {
-            o[8 + 2 * j] = p.U[j].real();
-            o[8 + 2 * j + 1] = p.U[j].imag();
+            o[16 + 2 * j] = p.U[j].real();
+            o[16 + 2 * j + 1] = p.U[j].imag();
+            o[528 + 2 * j] = p.V[j].real();
+            o[528 + 2 * j + 1] = p.V[j].imag();
           }
         }
       }

@@ -9,6 +9,7 @@ namespace dmg {
 
 struct PassInfo {
   int K, cls;
+  bool transpose;       // the in-place conjugate transpose (reference-order plans)
   size_t desc_off;      // byte offset of the descriptor in the device blob
   int tile_entries;
   unsigned grid;

@@ -7,8 +7,9 @@
 // Monomial classes (MOVE/SIGNED/PHASE) fuse the permutation and the per-entry
 // factor into the store, so they cost no FP64 arithmetic beyond one complex
 // multiply (PHASE) and never more than one HBM read and write per entry.
-// DENSE/SPARSE apply U to the ket bits of each column and conj(U) to the bra
-// bits of each row, which is U (x) conj(U) on the 2K target bits.
+// DENSE/SPARSE apply U to the ket bits of each column and V to the bra bits
+// of each row; V = conj(U) makes the pass U (x) conj(U) on the 2K target bits,
+// V = I makes it a ket-only pass (the reference's forward/backward stages).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -49,12 +50,15 @@ __global__ void __launch_bounds__(kThreads) k_pass(T* __restrict__ re, T* __rest
   __shared__ int s_lket[4], s_lbra[4];
   __shared__ T s_ure[(CLS == CLS_DENSE || CLS == CLS_SPARSE) ? D * D : 1];
   __shared__ T s_uim[(CLS == CLS_DENSE || CLS == CLS_SPARSE) ? D * D : 1];
+  __shared__ T s_vre[(CLS == CLS_DENSE || CLS == CLS_SPARSE) ? D * D : 1];
+  __shared__ T s_vim[(CLS == CLS_DENSE || CLS == CLS_SPARSE) ? D * D : 1];
   __shared__ T s_fre[CLS == CLS_PHASE ? D * D : 1];
   __shared__ T s_fim[CLS == CLS_PHASE ? D * D : 1];
   __shared__ int8_t s_fk[D * D];
-  __shared__ int8_t s_src[D];
-  __shared__ int8_t s_nnz[D];
+  __shared__ int8_t s_src[D], s_srcb[D];
+  __shared__ int8_t s_nnz[D], s_nnzb[D];
   __shared__ int8_t s_col[CLS == CLS_SPARSE ? D * D : 1];
+  __shared__ int8_t s_colb[CLS == CLS_SPARSE ? D * D : 1];
   __shared__ T s_rl[32];
 
   const int tid = threadIdx.x;
@@ -88,15 +92,22 @@ __global__ void __launch_bounds__(kThreads) k_pass(T* __restrict__ re, T* __rest
     s_lk[tid] = lk;
     s_lb[tid] = lb;
     s_src[tid] = dp->op.src[tid];
+    s_srcb[tid] = dp->op.srcb[tid];
     s_nnz[tid] = dp->op.nnz[tid];
+    s_nnzb[tid] = dp->op.nnzb[tid];
   }
   for (int i = tid; i < D * D; i += kThreads) {
     s_fk[i] = dp->op.fk[i];
     if (CLS == CLS_DENSE || CLS == CLS_SPARSE) {
       s_ure[i] = (T)dp->op.ure[i];
       s_uim[i] = (T)dp->op.uim[i];
+      s_vre[i] = (T)dp->op.vre[i];
+      s_vim[i] = (T)dp->op.vim[i];
     }
-    if (CLS == CLS_SPARSE) s_col[i] = dp->op.col[i];
+    if (CLS == CLS_SPARSE) {
+      s_col[i] = dp->op.col[i];
+      s_colb[i] = dp->op.colb[i];
+    }
     if (CLS == CLS_PHASE) {
       s_fre[i] = (T)dp->op.fre[i];
       s_fim[i] = (T)dp->op.fim[i];
@@ -200,7 +211,7 @@ __global__ void __launch_bounds__(kThreads) k_pass(T* __restrict__ re, T* __rest
         }
       }
       __syncthreads();
-      // ---- bra step: row (a, ., f) <- conj(U) row
+      // ---- bra step: row (a, ., f) <- V row (V = conj(U) for a superoperator pass)
       if (has_item) {
         const int a = r_item;
         const int ca = lf + s_lk[a];
@@ -223,11 +234,11 @@ __global__ void __launch_bounds__(kThreads) k_pass(T* __restrict__ re, T* __rest
             T ar = 0, ai = 0;
 #pragma unroll
             for (int c = 0; c < D; c++) {
-              const T ur = s_ure[b * D + c], ui = s_uim[b * D + c];
-              ar = fma(ur, xr[c], ar);
-              ar = fma(ui, xi[c], ar);
-              ai = fma(ur, xi[c], ai);
-              ai = fma(-ui, xr[c], ai);
+              const T vr = s_vre[b * D + c], vi = s_vim[b * D + c];
+              ar = fma(vr, xr[c], ar);
+              ar = fma(-vi, xi[c], ar);
+              ai = fma(vr, xi[c], ai);
+              ai = fma(vi, xr[c], ai);
             }
             sre[ca + s_lb[b]] = ar;
             sim[ca + s_lb[b]] = ai;
@@ -237,15 +248,15 @@ __global__ void __launch_bounds__(kThreads) k_pass(T* __restrict__ re, T* __rest
 #pragma unroll
           for (int b = 0; b < D; b++) {
             T ar = 0, ai = 0;
-            const int nz = s_nnz[b];
+            const int nz = s_nnzb[b];
             for (int j = 0; j < nz; j++) {
-              const int c = s_col[b * D + j];
-              const T ur = s_ure[b * D + c], ui = s_uim[b * D + c];
+              const int c = s_colb[b * D + j];
+              const T mr = s_vre[b * D + c], mi = s_vim[b * D + c];
               const T vr = sre[ca + s_lb[c]], vi = sim[ca + s_lb[c]];
-              ar = fma(ur, vr, ar);
-              ar = fma(ui, vi, ar);
-              ai = fma(ur, vi, ai);
-              ai = fma(-ui, vr, ai);
+              ar = fma(mr, vr, ar);
+              ar = fma(-mi, vi, ar);
+              ai = fma(mr, vi, ai);
+              ai = fma(mi, vr, ai);
             }
             yr[b] = ar;
             yi[b] = ai;
@@ -279,7 +290,7 @@ __global__ void __launch_bounds__(kThreads) k_pass(T* __restrict__ re, T* __rest
           const int loc = e + u;
           const int a = pext_local<K>(loc, s_lket);
           const int b = pext_local<K>(loc, s_lbra);
-          const int sa = s_src[a], sb = s_src[b];
+          const int sa = s_src[a], sb = s_srcb[b];
           const int sl = loc - s_lk[a] - s_lb[b] + s_lk[sa] + s_lb[sb];
           const T vr = sre[sl], vi = sim[sl];
           if (CLS == CLS_MOVE) {
@@ -392,6 +403,51 @@ int pass_blocks_per_sm(int K, int cls, bool fp32) {
     switch (K) { case 1: return occ_k<float, 1>(cls); case 2: return occ_k<float, 2>(cls); case 3: return occ_k<float, 3>(cls); default: return occ_k<float, 4>(cls); }
   }
   switch (K) { case 1: return occ_k<double, 1>(cls); case 2: return occ_k<double, 2>(cls); case 3: return occ_k<double, 3>(cls); default: return occ_k<double, 4>(cls); }
+}
+
+// ---------------------------------------------------------------- conj transpose
+// In place A'[x*dim + y] = conj(A[y*dim + x]): the reference's adjoint stage
+// between its forward and backward passes (block_transpose,
+// src/dmsim_nvgpu_omp.cuh:825-855), done as swaps of tile pairs (I, J), I <= J,
+// staged in shared memory so both the loads and the stores are coalesced.
+template <typename T>
+__global__ void __launch_bounds__(256) k_conj_transpose(T* __restrict__ re, T* __restrict__ im, int n) {
+  constexpr int TS = 32;
+  __shared__ T a_re[TS][TS + 1], a_im[TS][TS + 1], b_re[TS][TS + 1], b_im[TS][TS + 1];
+  const uint64_t dim = 1ull << n;
+  const int ts = dim < TS ? (int)dim : TS;
+  const uint64_t nt = dim / ts;
+  const int tx = threadIdx.x & 31, ty0 = threadIdx.x >> 5;  // 32 x 8 threads
+  for (uint64_t p = blockIdx.x; p < nt * nt; p += gridDim.x) {
+    const uint64_t I = p / nt, J = p % nt;
+    if (I > J) continue;  // uniform over the block
+    if (tx < ts)
+      for (int ty = ty0; ty < ts; ty += 8) {
+        const uint64_t ia = (I * ts + ty) * dim + J * ts + tx;  // tile (I,J)
+        const uint64_t ib = (J * ts + ty) * dim + I * ts + tx;  // tile (J,I)
+        a_re[ty][tx] = re[ia];
+        a_im[ty][tx] = im[ia];
+        b_re[ty][tx] = re[ib];
+        b_im[ty][tx] = im[ib];
+      }
+    __syncthreads();
+    if (tx < ts)
+      for (int ty = ty0; ty < ts; ty += 8) {
+        const uint64_t ia = (I * ts + ty) * dim + J * ts + tx;
+        const uint64_t ib = (J * ts + ty) * dim + I * ts + tx;
+        re[ia] = b_re[tx][ty];
+        im[ia] = flip(b_im[tx][ty]);
+        re[ib] = a_re[tx][ty];
+        im[ib] = flip(a_im[tx][ty]);
+      }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_conj_transpose(void* re, void* im, int n, bool fp32, unsigned grid, cudaStream_t s) {
+  if (fp32) k_conj_transpose<float><<<grid, 256, 0, s>>>((float*)re, (float*)im, n);
+  else k_conj_transpose<double><<<grid, 256, 0, s>>>((double*)re, (double*)im, n);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------- utilities

@@ -19,6 +19,8 @@ struct LaunchArgs {
 cudaError_t launch_pass(const LaunchArgs& a, cudaStream_t s);
 // Resident blocks per SM of the kernel instance for (K, cls, precision).
 int pass_blocks_per_sm(int K, int cls, bool fp32);
+// In place A'[x*2^n + y] = conj(A[y*2^n + x]) (the reference's adjoint stage)
+cudaError_t launch_conj_transpose(void* re, void* im, int n, bool fp32, unsigned grid, cudaStream_t s);
 // rho <- |0..0><0..0|
 cudaError_t launch_set_zero_state(void* re, void* im, uint64_t N, bool fp32, cudaStream_t s);
 // d_out[i] = Re rho[i][i] (FP64 whatever the state precision)

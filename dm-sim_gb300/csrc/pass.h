@@ -50,17 +50,20 @@ struct PassHeader {
   uint32_t stmask[8];   // bit h set: run h is written (it holds an entry the pass changes)
 };
 
-// Operator payload for width K (D = 2^K).
+// Operator payload for width K (D = 2^K).  A pass applies U to the ket
+// sub-index and V to the bra sub-index; a superoperator pass has V = conj(U),
+// a ket-only pass (the reference's forward/backward stages) has V = I.
 template <int K>
 struct PassOp {
   static constexpr int D = 1 << K;
   double ure[D * D], uim[D * D];   // U row-major (DENSE/SPARSE)
-  double fre[D * D], fim[D * D];   // f[a*D+b] = p_a * conj(p_b) (PHASE)
-  double rlin[16];                 // RLIN: ket 4x4 real map on (r0,i0,r1,i1); rlin-bar follows
-  double rlinb[16];
-  int8_t nnz[D];                   // SPARSE: nonzeros per row
-  int8_t col[D * D];               // SPARSE: column list per row
-  int8_t src[D];                   // monomial: source index of row a (U[a][src[a]] != 0)
+  double vre[D * D], vim[D * D];   // V row-major (DENSE/SPARSE)
+  double fre[D * D], fim[D * D];   // f[a*D+b] = U[a][src a] * V[b][srcb b] (PHASE)
+  double rlin[16];                 // RLIN: ket 4x4 real map on (r0,i0,r1,i1)
+  double rlinb[16];                // RLIN: bra 4x4 real map
+  int8_t nnz[D], nnzb[D];          // SPARSE: nonzeros per row of U and of V
+  int8_t col[D * D], colb[D * D];  // SPARSE: column lists per row
+  int8_t src[D], srcb[D];          // monomial: source index of row a of U / row b of V
   int8_t fk[D * D];                // monomial: factor kind of f[a][b]
 };
 

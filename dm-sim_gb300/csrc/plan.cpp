@@ -79,6 +79,40 @@ std::vector<PassSpec> plan_plain(const std::vector<Basic>& basics) {
   return out;
 }
 
+std::vector<PassSpec> plan_reference_order(const std::vector<Basic>& basics) {
+  std::vector<PassSpec> fwd;
+  for (const Basic& b : basics) {
+    PassSpec p;
+    p.nbasic = 1;
+    p.ket_only = true;
+    if (b.kind == BK_RLIN) {
+      p.K = 1;
+      p.q[0] = b.q[0];
+      p.rlin = true;
+      std::memcpy(p.rl, b.rl, sizeof p.rl);
+      for (int i = 0; i < 16; i++) p.rlb[i] = (i / 4 == i % 4) ? 1.0 : 0.0;
+      p.cls = CLS_RLIN;
+    } else {
+      p.K = nq(b);
+      p.q[0] = b.q[0];
+      if (p.K == 2) p.q[1] = b.q[1];
+      const int D = 1 << p.K;
+      for (int i = 0; i < D * D; i++) p.U[i] = b.u[i];
+      classify(p, false);
+    }
+    fwd.push_back(p);
+  }
+  std::vector<PassSpec> out = fwd;
+  PassSpec t;
+  t.transpose = true;
+  t.K = 0;
+  t.nbasic = 0;
+  out.push_back(t);
+  for (PassSpec& p : fwd) p.nbasic = 0;  // the second stage re-applies the same gates
+  out.insert(out.end(), fwd.begin(), fwd.end());
+  return out;
+}
+
 std::vector<PassSpec> plan_greedy(const std::vector<Basic>& basics, int maxk) {
   std::vector<PassSpec> out;
   const int m = (int)basics.size();
@@ -205,31 +239,38 @@ void classify(PassSpec& p, bool fused) {
   const int D = 1 << p.K;
   if (fused)
     for (int i = 0; i < D * D; i++) p.U[i] = cplx(snap1(p.U[i].real(), kSnapFused), snap1(p.U[i].imag(), kSnapFused));
-  int nnz = 0;
-  bool mono = true;
-  std::vector<int> colcount(D, 0);
-  for (int a = 0; a < D; a++) {
-    int rn = 0;
+  for (int i = 0; i < D * D; i++) p.V[i] = p.ket_only ? cplx(i / D == i % D ? 1.0 : 0.0, 0.0) : std::conj(p.U[i]);
+  auto count = [&](const cplx* M, bool& mono) {
+    int nnz = 0;
+    mono = true;
+    std::vector<int> colcount(D, 0);
+    for (int a = 0; a < D; a++) {
+      int rn = 0;
+      for (int c = 0; c < D; c++)
+        if (M[a * D + c] != cplx(0, 0)) {
+          rn++;
+          colcount[c]++;
+        }
+      nnz += rn;
+      if (rn != 1) mono = false;
+    }
     for (int c = 0; c < D; c++)
-      if (p.U[a * D + c] != cplx(0, 0)) {
-        rn++;
-        colcount[c]++;
-      }
-    nnz += rn;
-    if (rn != 1) mono = false;
-  }
-  for (int c = 0; c < D; c++)
-    if (colcount[c] != 1) mono = false;
+      if (colcount[c] != 1) mono = false;
+    return nnz;
+  };
+  bool mono_u, mono_v;
+  const int nnz = count(p.U, mono_u);
+  count(p.V, mono_v);
   p.nnz = nnz;
-  if (mono) {
+  if (mono_u && mono_v) {
     bool all_one = true, all_signed = true;
     for (int a = 0; a < D; a++) {
       int sa = 0;
       while (p.U[a * D + sa] == cplx(0, 0)) sa++;
       for (int b = 0; b < D; b++) {
         int sb = 0;
-        while (p.U[b * D + sb] == cplx(0, 0)) sb++;
-        const cplx f = p.U[a * D + sa] * std::conj(p.U[b * D + sb]);
+        while (p.V[b * D + sb] == cplx(0, 0)) sb++;
+        const cplx f = p.U[a * D + sa] * p.V[b * D + sb];
         const double fr = snap1(f.real(), kSnapFactor), fi = snap1(f.imag(), kSnapFactor);
         const bool one = fr == 1.0 && fi == 0.0;
         const bool sgn = one || (fr == -1.0 && fi == 0.0) || (fr == 0.0 && (fi == 1.0 || fi == -1.0));
@@ -301,10 +342,12 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
   for (int i = 0; i < D * D; i++) {
     op.ure[i] = p.U[i].real();
     op.uim[i] = p.U[i].imag();
+    op.vre[i] = p.V[i].real();
+    op.vim[i] = p.V[i].imag();
   }
   std::memcpy(op.rlin, p.rl, sizeof op.rlin);
   std::memcpy(op.rlinb, p.rlb, sizeof op.rlinb);
-  int src[kMaxD];
+  int src[kMaxD], srcb[kMaxD];
   for (int a = 0; a < D; a++) {
     int j = 0;
     for (int c = 0; c < D; c++)
@@ -312,13 +355,19 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
     op.nnz[a] = (int8_t)j;
     src[a] = j > 0 ? op.col[a * D] : a;
     op.src[a] = (int8_t)src[a];
+    int jb = 0;
+    for (int c = 0; c < D; c++)
+      if (p.V[a * D + c] != cplx(0, 0)) op.colb[a * D + jb++] = (int8_t)c;
+    op.nnzb[a] = (int8_t)jb;
+    srcb[a] = jb > 0 ? op.colb[a * D] : a;
+    op.srcb[a] = (int8_t)srcb[a];
   }
   const bool mono = p.cls == CLS_MOVE || p.cls == CLS_SIGNED || p.cls == CLS_PHASE;
   for (int a = 0; a < D; a++)
     for (int b = 0; b < D; b++) {
       int8_t fk = FK_GEN;
       if (mono) {
-        const cplx f = p.U[a * D + src[a]] * std::conj(p.U[b * D + src[b]]);
+        const cplx f = p.U[a * D + src[a]] * p.V[b * D + srcb[b]];
         const double fr = snap1(f.real(), kSnapFactor), fi = snap1(f.imag(), kSnapFactor);
         op.fre[a * D + b] = fr;
         op.fim[a * D + b] = fi;
@@ -344,9 +393,9 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
     }
     return r;
   };
-  auto row_identity = [&](int a) {
+  auto row_identity = [&](const cplx* M, int a) {
     for (int c = 0; c < D; c++)
-      if (p.U[a * D + c] != (c == a ? cplx(1, 0) : cplx(0, 0))) return false;
+      if (M[a * D + c] != (c == a ? cplx(1, 0) : cplx(0, 0))) return false;
     return true;
   };
   std::vector<char> st(1 << h.mhi, 0), ld(1 << h.mhi, 0);
@@ -354,8 +403,8 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
     for (int b = 0; b < D; b++) {
       bool changed;
       if (p.cls == CLS_RLIN) changed = true;
-      else if (mono) changed = src[a] != a || src[b] != b || op.fk[a * D + b] != FK_ONE;
-      else changed = !(row_identity(a) && row_identity(b));
+      else if (mono) changed = src[a] != a || srcb[b] != b || op.fk[a * D + b] != FK_ONE;
+      else changed = !(row_identity(p.U, a) && row_identity(p.V, b));
       if (changed) st[run_of(a, b)] = 1;
     }
   for (int a = 0; a < D; a++)
@@ -366,12 +415,12 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
         for (int a2 = 0; a2 < D; a2++)
           for (int b2 = 0; b2 < D; b2++) ld[run_of(a2, b2)] = 1;
       } else if (mono) {
-        ld[run_of(src[a], src[b])] = 1;
+        ld[run_of(src[a], srcb[b])] = 1;
       } else {
         for (int c = 0; c < D; c++) {
           if (p.U[a * D + c] == cplx(0, 0)) continue;
           for (int e = 0; e < D; e++)
-            if (p.U[b * D + e] != cplx(0, 0)) ld[run_of(c, e)] = 1;
+            if (p.V[b * D + e] != cplx(0, 0)) ld[run_of(c, e)] = 1;
         }
       }
     }

@@ -14,7 +14,10 @@ namespace dmg {
 struct PassSpec {
   int K = 0;
   int q[kMaxK] = {0, 0, 0, 0};
-  cplx U[kMaxD * kMaxD];       // row-major D x D
+  cplx U[kMaxD * kMaxD];       // ket operator, row-major D x D
+  cplx V[kMaxD * kMaxD];       // bra operator: conj(U) for a superoperator pass, I for a ket-only pass
+  bool ket_only = false;
+  bool transpose = false;      // not an operator: the in-place conjugate transpose of rho
   bool rlin = false;
   double rl[16], rlb[16];
   int cls = CLS_DENSE;
@@ -37,8 +40,14 @@ struct PassFeatures {
 //   (prefer gates inside the current qubit set), the fixed-width planner.
 std::vector<PassSpec> plan_plain(const std::vector<Basic>& basics);
 std::vector<PassSpec> plan_greedy(const std::vector<Basic>& basics, int maxk);
+// The reference's own order for circuits holding a real-linear gate (SRN):
+// every gate on the ket bits only, the conjugate transpose, every gate again
+// (src/dmsim_nvgpu_omp.cuh:918-969).  For complex-linear circuits and a
+// Hermitian rho this equals plan_plain; with SRN only this order matches.
+std::vector<PassSpec> plan_reference_order(const std::vector<Basic>& basics);
 
-// Snap near-exact entries, detect the arithmetic class.
+// Snap near-exact entries, set V = conj(U) (unless ket_only), detect the
+// arithmetic class.
 void classify(PassSpec& p, bool fused);
 
 // Size in bytes of the device descriptor of a width-K pass.

@@ -270,7 +270,7 @@ class Simulation:
         return re.value, im.value
 
 
-PASS_REC = 520
+PASS_REC = 1040
 
 
 def plan_inspect(n, circuit, mode="fused", max_k=4, planner="greedy"):
@@ -309,13 +309,17 @@ def plan_inspect(n, circuit, mode="fused", max_k=4, planner="greedy"):
         K = int(r[0])
         D = 1 << K
         rec = {"K": K, "cls": CLASS_NAMES[int(r[1])], "nbasic": int(r[2]), "nnz": int(r[3]),
-               "qubits": [int(x) for x in r[4:4 + K]]}
-        if rec["cls"] == "RLIN":
-            rec["rl"] = r[8:24].reshape(4, 4).copy()
-            rec["rlb"] = r[24:40].reshape(4, 4).copy()
+               "qubits": [int(x) for x in r[4:4 + K]], "ket_only": bool(r[8]), "transpose": bool(r[9])}
+        if rec["transpose"]:
+            rec["cls"] = "TRANSPOSE"
+        elif rec["cls"] == "RLIN":
+            rec["rl"] = r[16:32].reshape(4, 4).copy()
+            rec["rlb"] = r[528:544].reshape(4, 4).copy()
         else:
-            u = r[8:8 + 2 * D * D]
+            u = r[16:16 + 2 * D * D]
+            v = r[528:528 + 2 * D * D]
             rec["U"] = (u[0::2] + 1j * u[1::2]).reshape(D, D)
+            rec["V"] = (v[0::2] + 1j * v[1::2]).reshape(D, D)
         passes.append(rec)
     return passes
 

@@ -114,12 +114,14 @@ int dmsim_alloc_host(size_t bytes, void** out);
 int dmsim_free_host(void* p);
 /* Host-only planning (no GPU needed): decompose and plan a circuit exactly as
  * dmsim_upload would and return, per pass, DMSIM_PASS_REC doubles:
- * {K, class, n_basic, nnz, q0, q1, q2, q3} followed by the 16x16 complex
- * operator (re/im interleaved, row stride 2^K; for the real-linear class the
- * ket map then the bra map, 16 doubles each).  ops[i], qubits[5*i..], params
- * [3*i..] = theta, phi, lambda; mats[32*i..] holds C1/C2 matrices (may be NULL
- * when there are none).  Returns the pass count in *npasses. */
-#define DMSIM_PASS_REC 520
+ * [0..7] {K, class, n_basic, nnz, q0, q1, q2, q3}, [8] ket-only flag,
+ * [9] transpose flag (the reference-order adjoint stage, no operator),
+ * [16..527] the ket operator U and [528..1039] the bra operator V (16x16
+ * complex, re/im interleaved, row stride 2^K; for the real-linear class the
+ * 4x4 real ket and bra maps).  ops[i], qubits[5*i..], params[3*i..] = theta,
+ * phi, lambda; mats[32*i..] holds C1/C2 matrices (may be NULL when there are
+ * none).  Returns the pass count in *npasses. */
+#define DMSIM_PASS_REC 1040
 int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qubits, const double* params,
                        const double* mats, uint32_t ngates, int mode, int max_k, int planner,
                        double* out, uint32_t cap, uint32_t* npasses);

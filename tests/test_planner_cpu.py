@@ -9,7 +9,11 @@ import dmsim_workloads as W
 
 
 def apply_pass_dm(rho, n, p):
-    """rho[r][c]; apply the pass to ket (rows) and bra (columns)."""
+    """rho[r][c]; apply the pass: U to the ket (rows) and V to the bra (columns),
+    rho' = U rho V^T (V = conj(U) for a superoperator pass, I for a ket-only
+    pass); the transpose stage is rho' = rho^dagger."""
+    if p["cls"] == "TRANSPOSE":
+        return rho.conj().T.copy()
     K, qs = p["K"], p["qubits"]
     d = 1 << n
     t = rho.reshape([2] * (2 * n))  # axes: row bits (n-1 .. 0), then col bits (n-1 .. 0)
@@ -39,7 +43,8 @@ def apply_pass_dm(rho, n, p):
     t = np.tensordot(Ut, t, axes=(in_axes, ax_row))
     t = np.moveaxis(t, out_axes, ax_row)
     ax_col = [col_ax[K - 1 - i] for i in range(K)]
-    t = np.tensordot(Ut.conj(), t, axes=(in_axes, ax_col))
+    Vt = p["V"].reshape([2] * (2 * K))
+    t = np.tensordot(Vt, t, axes=(in_axes, ax_col))
     t = np.moveaxis(t, out_axes, ax_col)
     return t.reshape(d, d)
 
@@ -68,6 +73,22 @@ def test_plan_reproduces_oracle(engine, oracle, mode, max_k, seed):
     assert all(p["K"] <= (2 if mode == "plain" else max(max_k, 2)) for p in passes)
     nb = sum(oracle.basic_count(g) for g in circ)
     assert sum(p["nbasic"] for p in passes) == nb - sum(1 for g in circ if g[0] == W.OP["ID"])
+
+
+@pytest.mark.parametrize("mode", ["plain", "fused"])
+def test_srn_circuits_follow_reference_order(engine, oracle, mode):
+    """SRN is real-linear (src/dmsim_nvgpu_omp.cuh:1253-1266); only the
+    reference's own order (all gates on the ket bits, conjugate transpose,
+    all gates again) reproduces its result, and a circuit holding SRN is
+    planned that way."""
+    n = 4
+    for seed in range(3):
+        circ = W.random_circuit(n, 40, seed=500 + seed)
+        circ.insert(5, (W.OP["SRN"], (seed % n,), 0.0, 0.0, 0.0))
+        rho, passes = run_plan(n, circ, mode, 4, engine)
+        assert sum(p["cls"] == "TRANSPOSE" for p in passes) == 1
+        re, im = oracle.dm_sim(n, circ)
+        assert np.abs(rho - oracle.rho_from_result(n, re, im)).max() < 1e-12
 
 
 def test_plain_classes(engine):
