@@ -1,0 +1,240 @@
+// costmodel.cpp -- the learned pass-time model (host side) and the planner that
+// uses it.  Training and inference run on the GPU through mlp.cu; the host only
+// builds feature vectors, moves them and reads the loss.
+#include "costmodel.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <random>
+
+namespace dmg {
+
+void pass_features(const PassFeatures& f, bool fp32, float* x) {
+  const double nb = 2.0 * f.n;
+  for (int i = 0; i < kMlpIn; i++) x[i] = 0.f;
+  x[0] = f.K / 4.0f;
+  if (f.cls >= 0 && f.cls < CLS_COUNT) x[1 + f.cls] = 1.f;  // x[1..6] class one-hot
+  const int D = 1 << f.K;
+  x[7] = (float)f.nnz / (float)(D * D);           // density of U
+  x[8] = (float)f.nnz / (float)D / 16.f;          // nonzeros per row
+  x[9] = (float)f.ld_frac;
+  x[10] = (float)f.st_frac;
+  x[11] = (float)((f.max_lo_bit + 1) / nb);
+  x[12] = (float)(f.min_hi_bit / nb);
+  x[13] = (float)(nb / 34.0);                     // log2 of the entry count
+  x[14] = fp32 ? 1.f : 0.f;
+  x[15] = (float)((f.nnz / (double)D) * f.ld_frac * std::ldexp(1.0, (int)nb - 28));  // arithmetic volume
+}
+
+CostModel& global_cost_model() {
+  static CostModel m;
+  return m;
+}
+
+namespace {
+constexpr uint32_t kMagic = 0x434d4d44;  // "DMMC"
+constexpr uint32_t kVersion = 1;
+}  // namespace
+
+bool cost_model_save(const CostModel& m, const std::string& path) {
+  FILE* f = fopen(path.c_str(), "wb");
+  if (!f) return false;
+  const uint32_t hdr[4] = {kMagic, kVersion, (uint32_t)kMlpIn, (uint32_t)kMlpParams};
+  bool ok = fwrite(hdr, sizeof hdr, 1, f) == 1;
+  ok = ok && fwrite(&m.y_mean, sizeof(float), 1, f) == 1 && fwrite(&m.y_std, sizeof(float), 1, f) == 1;
+  ok = ok && fwrite(m.params, sizeof(float), kMlpParams, f) == (size_t)kMlpParams;
+  fclose(f);
+  return ok;
+}
+
+bool cost_model_load(CostModel& m, const std::string& path) {
+  FILE* f = fopen(path.c_str(), "rb");
+  if (!f) return false;
+  uint32_t hdr[4];
+  bool ok = fread(hdr, sizeof hdr, 1, f) == 1 && hdr[0] == kMagic && hdr[1] == kVersion && hdr[2] == (uint32_t)kMlpIn &&
+            hdr[3] == (uint32_t)kMlpParams;
+  CostModel t;
+  ok = ok && fread(&t.y_mean, sizeof(float), 1, f) == 1 && fread(&t.y_std, sizeof(float), 1, f) == 1;
+  ok = ok && fread(t.params, sizeof(float), kMlpParams, f) == (size_t)kMlpParams;
+  fclose(f);
+  if (!ok) return false;
+  t.ready = true;
+  m = t;
+  return true;
+}
+
+void cost_model_init(CostModel& m, uint64_t seed) {
+  std::mt19937_64 rng(seed);
+  std::normal_distribution<float> nd(0.f, 1.f);
+  const int I = kMlpIn, H = kMlpHidden;
+  int o = 0;
+  for (int i = 0; i < H * I; i++) m.params[o++] = nd(rng) * std::sqrt(2.f / I);
+  for (int i = 0; i < H; i++) m.params[o++] = 0.f;
+  for (int i = 0; i < H * H; i++) m.params[o++] = nd(rng) * std::sqrt(2.f / H);
+  for (int i = 0; i < H; i++) m.params[o++] = 0.f;
+  for (int i = 0; i < H; i++) m.params[o++] = nd(rng) * std::sqrt(1.f / H);
+  m.params[o++] = 0.f;
+  m.y_mean = 0.f;
+  m.y_std = 1.f;
+  m.ready = false;
+}
+
+namespace {
+struct DevBuf {
+  void* p = nullptr;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t alloc(size_t n) { return cudaMalloc(&p, n); }
+  float* f() { return static_cast<float*>(p); }
+};
+#define CM_CUDA(x)                                   \
+  do {                                               \
+    cudaError_t e_ = (x);                            \
+    if (e_ != cudaSuccess) {                         \
+      err = std::string(#x) + ": " + cudaGetErrorString(e_); \
+      return false;                                  \
+    }                                                \
+  } while (0)
+}  // namespace
+
+bool cost_model_train(CostModel& m, const std::vector<float>& X, const std::vector<float>& ms, int steps, float lr,
+                      float loss[2], std::string& err) {
+  const int B = (int)ms.size();
+  if (B == 0 || (int)X.size() != B * kMlpIn) {
+    err = "empty or mismatched training set";
+    return false;
+  }
+  // standardised log-time targets
+  std::vector<float> T(B);
+  double mean = 0, var = 0;
+  for (int i = 0; i < B; i++) {
+    T[i] = std::log(std::max(ms[i], 1e-6f));
+    mean += T[i];
+  }
+  mean /= B;
+  for (int i = 0; i < B; i++) var += (T[i] - mean) * (T[i] - mean);
+  const double sd = std::sqrt(var / B) + 1e-6;
+  for (int i = 0; i < B; i++) T[i] = (float)((T[i] - mean) / sd);
+  m.y_mean = (float)mean;
+  m.y_std = (float)sd;
+
+  cudaStream_t s;
+  CM_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  DevBuf dp, dX, dT, dg, dm, dv, dl;
+  bool ok = true;
+  auto fail = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && ok) {
+      err = std::string(what) + ": " + cudaGetErrorString(e);
+      ok = false;
+    }
+  };
+  fail(dp.alloc(kMlpParams * 4), "alloc");
+  fail(dX.alloc((size_t)B * kMlpIn * 4), "alloc");
+  fail(dT.alloc((size_t)B * 4), "alloc");
+  fail(dg.alloc(kMlpParams * 4), "alloc");
+  fail(dm.alloc(kMlpParams * 4), "alloc");
+  fail(dv.alloc(kMlpParams * 4), "alloc");
+  fail(dl.alloc(4), "alloc");
+  if (ok) {
+    fail(cudaMemcpyAsync(dp.p, m.params, kMlpParams * 4, cudaMemcpyHostToDevice, s), "copy");
+    fail(cudaMemcpyAsync(dX.p, X.data(), (size_t)B * kMlpIn * 4, cudaMemcpyHostToDevice, s), "copy");
+    fail(cudaMemcpyAsync(dT.p, T.data(), (size_t)B * 4, cudaMemcpyHostToDevice, s), "copy");
+    fail(cudaMemsetAsync(dm.p, 0, kMlpParams * 4, s), "memset");
+    fail(cudaMemsetAsync(dv.p, 0, kMlpParams * 4, s), "memset");
+  }
+  for (int t = 1; ok && t <= steps; t++) {
+    fail(mlp_grad(dp.f(), dX.f(), dT.f(), B, dg.f(), dl.f(), s), "mlp_grad");
+    if (t == 1) {
+      fail(cudaMemcpyAsync(&loss[0], dl.p, 4, cudaMemcpyDeviceToHost, s), "copy");
+    }
+    fail(mlp_adam(dp.f(), dg.f(), dm.f(), dv.f(), lr, t, s), "mlp_adam");
+  }
+  if (ok) {
+    fail(mlp_grad(dp.f(), dX.f(), dT.f(), B, dg.f(), dl.f(), s), "mlp_grad");
+    fail(cudaMemcpyAsync(&loss[1], dl.p, 4, cudaMemcpyDeviceToHost, s), "copy");
+    fail(cudaMemcpyAsync(m.params, dp.p, kMlpParams * 4, cudaMemcpyDeviceToHost, s), "copy");
+    fail(cudaStreamSynchronize(s), "sync");
+  }
+  cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  if (ok) m.ready = true;
+  return ok;
+}
+
+bool cost_model_predict(const CostModel& m, const std::vector<float>& X, std::vector<float>& ms, std::string& err) {
+  const int B = (int)(X.size() / kMlpIn);
+  ms.assign(B, 0.f);
+  if (B == 0) return true;
+  if (!m.ready) {
+    err = "the cost model is not trained or loaded";
+    return false;
+  }
+  cudaStream_t s;
+  CM_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  DevBuf dp, dX, dy;
+  bool ok = true;
+  auto fail = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && ok) {
+      err = std::string(what) + ": " + cudaGetErrorString(e);
+      ok = false;
+    }
+  };
+  fail(dp.alloc(kMlpParams * 4), "alloc");
+  fail(dX.alloc((size_t)B * kMlpIn * 4), "alloc");
+  fail(dy.alloc((size_t)B * 4), "alloc");
+  if (ok) {
+    fail(cudaMemcpyAsync(dp.p, m.params, kMlpParams * 4, cudaMemcpyHostToDevice, s), "copy");
+    fail(cudaMemcpyAsync(dX.p, X.data(), (size_t)B * kMlpIn * 4, cudaMemcpyHostToDevice, s), "copy");
+    fail(mlp_forward(dp.f(), dX.f(), B, dy.f(), s), "mlp_forward");
+    fail(cudaMemcpyAsync(ms.data(), dy.p, (size_t)B * 4, cudaMemcpyDeviceToHost, s), "copy");
+    fail(cudaStreamSynchronize(s), "sync");
+  }
+  cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  if (!ok) return false;
+  for (float& v : ms) v = std::exp(v * m.y_std + m.y_mean);
+  return true;
+}
+
+std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int maxk, bool fp32, const CostModel& m,
+                                   double* predicted_ms, std::string& err) {
+  // candidate plans: the unfused plan, and greedy plans of every width up to
+  // maxk under row-density caps
+  std::vector<std::vector<PassSpec>> cands;
+  cands.push_back(plan_plain(basics));
+  const int caps[] = {kMaxD, 8, 4, 2};
+  for (int k = 2; k <= maxk; k++)
+    for (int cap : caps) {
+      if (cap >= (1 << k) && cap != kMaxD) continue;  // no effect at this width
+      cands.push_back(plan_greedy(basics, k, cap));
+    }
+  // features of every pass of every candidate, one batched inference
+  std::vector<float> X;
+  std::vector<int> owner;
+  std::vector<unsigned char> buf(desc_size(kMaxK));
+  for (size_t c = 0; c < cands.size(); c++)
+    for (const PassSpec& p : cands[c]) {
+      PassFeatures f;
+      std::memset(&f, 0, sizeof f);
+      if (p.transpose) continue;
+      build_desc(p, n, buf.data(), &f, nullptr, nullptr);
+      float x[kMlpIn];
+      pass_features(f, fp32, x);
+      X.insert(X.end(), x, x + kMlpIn);
+      owner.push_back((int)c);
+    }
+  std::vector<float> ms;
+  if (!cost_model_predict(m, X, ms, err)) return {};
+  std::vector<double> tot(cands.size(), 0.0);
+  for (size_t i = 0; i < ms.size(); i++) tot[owner[i]] += ms[i];
+  const size_t best = (size_t)(std::min_element(tot.begin(), tot.end()) - tot.begin());
+  if (predicted_ms) *predicted_ms = tot[best];
+  return cands[best];
+}
+
+}  // namespace dmg

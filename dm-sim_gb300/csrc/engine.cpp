@@ -18,7 +18,12 @@
 #include <string>
 #include <vector>
 
+#include <dlfcn.h>
+
+#include <random>
+
 #include "../../include/dmsim_gb300.h"
+#include "costmodel.h"
 #include "engine_internal.h"
 #include "gates.h"
 #include "kernels.h"
@@ -67,7 +72,7 @@ struct dmsim_sim {
   int mode = 0, maxk = 4, planner = 0, record = 0, graph_on = 1, verbose = 0;
   int64_t seed = -1;
 
-  double last_ms = 0, last_bytes = 0;
+  double last_ms = 0, last_bytes = 0, predicted_ms = 0;
   std::vector<PassRecord> records;
   std::string err;
 };
@@ -149,6 +154,22 @@ void enqueue_passes(dmsim_sim* s, bool timed) {
   }
 }
 
+// The cost model shipped with the library: $DMSIM_COST_MODEL, else
+// <library dir>/../model/cost_mlp.bin.
+void load_default_cost_model() {
+  std::string path;
+  if (const char* e = getenv("DMSIM_COST_MODEL")) path = e;
+  if (path.empty()) {
+    Dl_info info;
+    if (dladdr(reinterpret_cast<void*>(&dmsim_create), &info) && info.dli_fname) {
+      std::string lib = info.dli_fname;
+      const size_t cut = lib.find_last_of('/');
+      path = (cut == std::string::npos ? std::string(".") : lib.substr(0, cut)) + "/../model/cost_mlp.bin";
+    }
+  }
+  if (!path.empty()) cost_model_load(global_cost_model(), path);
+}
+
 // Plain: one pass per basic gate.  Fused: the greedy (fixed-width) or the
 // learned planner.  A circuit holding a real-linear gate (SRN) runs in the
 // reference's own order in either mode, the only order that reproduces it.
@@ -157,17 +178,34 @@ std::vector<PassSpec> make_plan(dmsim_sim* s, const std::vector<Basic>& basics) 
   for (const Basic& b : basics) has_rlin |= b.kind == BK_RLIN;
   if (has_rlin) return plan_reference_order(basics);
   if (s->mode == 0) return plan_plain(basics);
-  if (s->planner == 1) throw DmError{DMSIM_ERR_UNSUPPORTED, "the learned planner is not available in this build"};
+  if (s->planner == 1) {
+    CostModel& m = global_cost_model();
+    if (!m.ready) load_default_cost_model();
+    if (!m.ready)
+      throw DmError{DMSIM_ERR_STATE, "the learned planner needs a cost model: train one (dmsim_cost_train) or load one "
+                                     "(dmsim_cost_load, or set DMSIM_COST_MODEL)"};
+    std::string err;
+    std::vector<PassSpec> p = plan_learned(basics, (int)s->n, s->maxk, s->fp32, m, &s->predicted_ms, err);
+    if (!err.empty()) throw DmError{DMSIM_ERR_CUDA, "learned planner: " + err};
+    return p;
+  }
   return plan_greedy(basics, s->maxk);
 }
+
+void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_basic);
 
 void upload(dmsim_sim* s) {
   if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "upload() called twice without clear_circuit() (:347-350)"};
   ensure_state(s);
   std::vector<Basic> basics;
   for (const GateRec& g : s->circuit) decompose(g, basics);
-  s->n_basic = (uint32_t)basics.size();
-  std::vector<PassSpec> specs = make_plan(s, basics);
+  upload_specs(s, make_plan(s, basics), (uint32_t)basics.size());
+}
+
+// Write the descriptors of a plan to the device and capture its launches.
+void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_basic) {
+  ensure_state(s);
+  s->n_basic = n_basic;
   // descriptors, 256-byte aligned, one host blob, one copy
   std::vector<size_t> offs;
   size_t total = 0;
@@ -712,8 +750,14 @@ int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qu
     std::vector<PassSpec> specs;
     if (has_rlin) specs = plan_reference_order(basics);
     else if (mode == 0) specs = plan_plain(basics);
-    else if (planner == 1) return DMSIM_ERR_UNSUPPORTED;
-    else specs = plan_greedy(basics, max_k);
+    else if (planner == 1) {
+      CostModel& m = global_cost_model();
+      if (!m.ready) load_default_cost_model();
+      if (!m.ready) return DMSIM_ERR_STATE;
+      std::string err;
+      specs = plan_learned(basics, (int)n_qubits, max_k, false, m, nullptr, err);
+      if (!err.empty()) return DMSIM_ERR_CUDA;
+    } else specs = plan_greedy(basics, max_k);
     if (npasses) *npasses = (uint32_t)specs.size();
     if (out)
       for (uint32_t i = 0; i < cap && i < specs.size(); i++) {
@@ -745,6 +789,170 @@ int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qu
     return DMSIM_ERR_ARG;
   }
   return DMSIM_OK;
+}
+
+// ---------------------------------------------------------------- cost model
+namespace {
+// Random circuit from the 29-entry mixed table (mt19937_64), in engine form.
+void random_table_circuit(uint32_t n, uint32_t ngates, std::mt19937_64& rng, std::vector<GateRec>& out) {
+  static const int table[] = {2, 1, 0, 13, 14, 15, 8, 9, 11, 5, 6, 7, 3, 17, 16, 19, 18, 22, 23, 24, 25, 26, 27, 37, 28,
+                              20, 21, 31, 33};
+  std::uniform_int_distribution<int> pick(0, (int)(sizeof(table) / sizeof(table[0])) - 1);
+  std::uniform_real_distribution<double> ang(0.0, 6.283185307179586);
+  for (uint32_t i = 0; i < ngates; i++) {
+    GateRec g;
+    std::memset(&g, 0, sizeof g);
+    int op = table[pick(rng)];
+    while (gate_arity(op) > (int)n) op = table[pick(rng)];
+    g.op = op;
+    std::vector<uint32_t> qs(n);
+    for (uint32_t q = 0; q < n; q++) qs[q] = q;
+    std::shuffle(qs.begin(), qs.end(), rng);
+    for (int k = 0; k < gate_arity(op); k++) g.qb[k] = qs[k];
+    g.theta = ang(rng);
+    g.phi = ang(rng);
+    g.lambda = ang(rng);
+    out.push_back(g);
+  }
+}
+}  // namespace
+
+int dmsim_cost_collect(uint32_t n, uint32_t n_circuits, uint32_t gates, uint64_t seed, double* feats, double* ms,
+                       uint32_t cap, uint32_t* count) {
+  if (!count || n < 2 || n > 16) return DMSIM_ERR_ARG;
+  *count = 0;
+  dmsim_handle h = nullptr;
+  int st = dmsim_create(n, 1, &h);
+  if (st != DMSIM_OK) return st;
+  std::mt19937_64 rng(seed);
+  uint32_t got = 0;
+  try {
+    h->record = 1;
+    h->graph_on = 0;
+    const int widths[] = {1, 2, 3, 4};
+    const int caps[] = {kMaxD, 8, 4, 2};
+    for (uint32_t c = 0; c < n_circuits; c++) {
+      std::vector<GateRec> circ;
+      random_table_circuit(n, gates, rng, circ);
+      std::vector<Basic> basics;
+      for (const GateRec& g : circ) decompose(g, basics);
+      for (int k : widths)
+        for (int rc : caps) {
+          if (rc != kMaxD && rc >= (1 << k)) continue;
+          std::vector<PassSpec> specs = k == 1 ? plan_plain(basics) : plan_greedy(basics, k, rc);
+          upload_specs(h, specs, (uint32_t)basics.size());
+          h->uploaded = true;
+          run(h);
+          for (const PassRecord& r : h->records) {
+            if (got < cap && feats && ms) {
+              float x[kMlpIn];
+              pass_features(r.feat, h->fp32, x);
+              for (int i = 0; i < kMlpIn; i++) feats[(size_t)got * kMlpIn + i] = x[i];
+              ms[got] = r.ms;
+            }
+            got++;
+          }
+          clear_circuit(h);
+          h->circuit.clear();
+          if (k == 1) break;
+        }
+    }
+  } catch (const DmError& e) {
+    dmsim_destroy(h);
+    return e.code;
+  }
+  dmsim_destroy(h);
+  *count = got;
+  return DMSIM_OK;
+}
+
+int dmsim_cost_train(const double* feats, const double* ms, uint32_t count, uint32_t steps, double lr, uint64_t seed,
+                     double loss[2]) {
+  if (!feats || !ms || count == 0) return DMSIM_ERR_ARG;
+  std::vector<float> X((size_t)count * kMlpIn), Y(count);
+  for (size_t i = 0; i < X.size(); i++) X[i] = (float)feats[i];
+  for (uint32_t i = 0; i < count; i++) Y[i] = (float)ms[i];
+  CostModel& m = global_cost_model();
+  cost_model_init(m, seed);
+  float l[2] = {0, 0};
+  std::string err;
+  if (!cost_model_train(m, X, Y, (int)steps, (float)lr, l, err)) {
+    fprintf(stderr, "dmsim_cost_train: %s\n", err.c_str());
+    return DMSIM_ERR_CUDA;
+  }
+  if (loss) {
+    loss[0] = l[0];
+    loss[1] = l[1];
+  }
+  return DMSIM_OK;
+}
+
+int dmsim_cost_predict(const double* feats, uint32_t count, double* out_ms) {
+  if (!feats || !out_ms) return DMSIM_ERR_ARG;
+  CostModel& m = global_cost_model();
+  if (!m.ready) load_default_cost_model();
+  if (!m.ready) return DMSIM_ERR_STATE;
+  std::vector<float> X((size_t)count * kMlpIn), Y;
+  for (size_t i = 0; i < X.size(); i++) X[i] = (float)feats[i];
+  std::string err;
+  if (!cost_model_predict(m, X, Y, err)) return DMSIM_ERR_CUDA;
+  for (uint32_t i = 0; i < count; i++) out_ms[i] = Y[i];
+  return DMSIM_OK;
+}
+
+int dmsim_cost_save(const char* path) {
+  if (!path || !global_cost_model().ready) return DMSIM_ERR_STATE;
+  return cost_model_save(global_cost_model(), path) ? DMSIM_OK : DMSIM_ERR_ARG;
+}
+
+int dmsim_cost_load(const char* path) {
+  if (!path) return DMSIM_ERR_ARG;
+  return cost_model_load(global_cost_model(), path) ? DMSIM_OK : DMSIM_ERR_ARG;
+}
+
+int dmsim_mlp_forward(const float* params, const float* X, uint32_t B, float* y) {
+  if (!params || !X || !y) return DMSIM_ERR_ARG;
+  float *dp = nullptr, *dX = nullptr, *dy = nullptr;
+  cudaError_t e = cudaMalloc(&dp, kMlpParams * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&dX, (size_t)std::max<uint32_t>(B, 1) * kMlpIn * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&dy, (size_t)std::max<uint32_t>(B, 1) * 4);
+  if (e == cudaSuccess) e = cudaMemcpy(dp, params, kMlpParams * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dX, X, (size_t)B * kMlpIn * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = mlp_forward(dp, dX, (int)B, dy, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(y, dy, (size_t)B * 4, cudaMemcpyDeviceToHost);
+  cudaFree(dp);
+  cudaFree(dX);
+  cudaFree(dy);
+  return e == cudaSuccess ? DMSIM_OK : DMSIM_ERR_CUDA;
+}
+
+int dmsim_mlp_grad(const float* params, const float* X, const float* T, uint32_t B, float* grad, float* loss) {
+  if (!params || !X || !T || !grad || !loss) return DMSIM_ERR_ARG;
+  float *dp = nullptr, *dX = nullptr, *dT = nullptr, *dg = nullptr, *dl = nullptr;
+  cudaError_t e = cudaMalloc(&dp, kMlpParams * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&dX, (size_t)std::max<uint32_t>(B, 1) * kMlpIn * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&dT, (size_t)std::max<uint32_t>(B, 1) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&dg, kMlpParams * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&dl, 4);
+  if (e == cudaSuccess) e = cudaMemcpy(dp, params, kMlpParams * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dX, X, (size_t)B * kMlpIn * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dT, T, (size_t)B * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = mlp_grad(dp, dX, dT, (int)B, dg, dl, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(grad, dg, kMlpParams * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(loss, dl, 4, cudaMemcpyDeviceToHost);
+  cudaFree(dp);
+  cudaFree(dX);
+  cudaFree(dT);
+  cudaFree(dg);
+  cudaFree(dl);
+  return e == cudaSuccess ? DMSIM_OK : DMSIM_ERR_CUDA;
+}
+
+int dmsim_plan_predicted_ms(dmsim_handle s, double* ms) {
+  DM_TRY(s, {
+    if (!ms) throw DmError{DMSIM_ERR_ARG, "null output"};
+    *ms = s->predicted_ms;
+  });
 }
 
 const char* dmsim_last_error(dmsim_handle s) { return s ? s->err.c_str() : "null handle"; }

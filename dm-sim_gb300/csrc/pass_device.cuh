@@ -1,0 +1,337 @@
+// pass_device.cuh -- the device side of one superoperator pass, shared by the
+// per-pass kernel (kernels.cu) and the batched work-queue kernel (batch.cu).
+//
+// A block owns one tile at a time: it loads the tile's touched runs with
+// 16-byte vector loads into shared memory, transforms them, and stores them
+// back.  Monomial classes (MOVE/SIGNED/PHASE) fuse the permutation and the
+// per-entry factor into the store, so they cost at most one complex multiply
+// per entry.  DENSE/SPARSE apply U to the ket bits of each column and V to the
+// bra bits of each row; V = conj(U) makes the pass U (x) conj(U) on the 2K
+// target bits, V = I makes it a ket-only pass (the reference's forward and
+// backward stages).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pass.h"
+
+namespace dmg {
+
+template <typename T> struct Vec2;
+template <> struct Vec2<double> { using type = double2; };
+template <> struct Vec2<float> { using type = float2; };
+
+// Sign flip on the integer pipe (GB300's FP64 pipe is ~1/58 of the FP32 rate).
+__device__ __forceinline__ double flip(double x) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
+__device__ __forceinline__ float flip(float x) { return __int_as_float(__float_as_int(x) ^ (int)0x80000000); }
+
+template <int K>
+__device__ __forceinline__ int pext_local(int loc, const int* lpos) {
+  int a = 0;
+#pragma unroll
+  for (int i = 0; i < K; i++) a |= ((loc >> lpos[i]) & 1) << i;
+  return a;
+}
+
+// Per-pass constant tables, staged in shared memory once per block (or once
+// per work-queue range).  Arrays a class does not use shrink to one element.
+template <typename T, int K, int CLS>
+struct PassTables {
+  static constexpr int D = 1 << K;
+  static constexpr bool kMat = CLS == CLS_DENSE || CLS == CLS_SPARSE;
+  uint64_t hioff[256];
+  uint32_t ldmask[8], stmask[8];
+  int lk[D], lb[D];
+  int lket[4], lbra[4];
+  T ure[kMat ? D * D : 1], uim[kMat ? D * D : 1], vre[kMat ? D * D : 1], vim[kMat ? D * D : 1];
+  T fre[CLS == CLS_PHASE ? D * D : 1], fim[CLS == CLS_PHASE ? D * D : 1];
+  T rl[32];
+  int8_t fk[D * D];
+  int8_t src[D], srcb[D], nnz[D], nnzb[D];
+  int8_t col[CLS == CLS_SPARSE ? D * D : 1], colb[CLS == CLS_SPARSE ? D * D : 1];
+};
+
+template <typename T, int K, int CLS>
+constexpr size_t pass_smem_bytes(int tile_entries) {
+  return (((size_t)2 * tile_entries * sizeof(T) + 15) & ~(size_t)15) + sizeof(PassTables<T, K, CLS>);
+}
+
+// All threads of the block; the caller synchronises afterwards.
+template <typename T, int K, int CLS>
+__device__ void load_tables(const PassDesc<K>* __restrict__ dp, PassTables<T, K, CLS>& tb) {
+  constexpr int D = 1 << K;
+  const int tid = threadIdx.x;
+  const PassHeader& h = dp->h;
+  const int mhi = h.mhi;
+  for (int r = tid; r < (1 << mhi); r += blockDim.x) {
+    uint64_t off = 0;
+    for (int j = 0; j < mhi; j++) off |= (uint64_t)((r >> j) & 1) << h.hipos[j];
+    tb.hioff[r] = off;
+  }
+  if (tid < 8) {
+    tb.ldmask[tid] = h.ldmask[tid];
+    tb.stmask[tid] = h.stmask[tid];
+  }
+  if (tid < K) {
+    tb.lket[tid] = h.lket[tid];
+    tb.lbra[tid] = h.lbra[tid];
+  }
+  if (tid < D) {
+    int lk = 0, lb = 0;
+    for (int i = 0; i < K; i++) {
+      lk |= ((tid >> i) & 1) << h.lket[i];
+      lb |= ((tid >> i) & 1) << h.lbra[i];
+    }
+    tb.lk[tid] = lk;
+    tb.lb[tid] = lb;
+    tb.src[tid] = dp->op.src[tid];
+    tb.srcb[tid] = dp->op.srcb[tid];
+    tb.nnz[tid] = dp->op.nnz[tid];
+    tb.nnzb[tid] = dp->op.nnzb[tid];
+  }
+  for (int i = tid; i < D * D; i += blockDim.x) {
+    tb.fk[i] = dp->op.fk[i];
+    if (PassTables<T, K, CLS>::kMat) {
+      tb.ure[i] = (T)dp->op.ure[i];
+      tb.uim[i] = (T)dp->op.uim[i];
+      tb.vre[i] = (T)dp->op.vre[i];
+      tb.vim[i] = (T)dp->op.vim[i];
+    }
+    if (CLS == CLS_SPARSE) {
+      tb.col[i] = dp->op.col[i];
+      tb.colb[i] = dp->op.colb[i];
+    }
+    if (CLS == CLS_PHASE) {
+      tb.fre[i] = (T)dp->op.fre[i];
+      tb.fim[i] = (T)dp->op.fim[i];
+    }
+  }
+  if (CLS == CLS_RLIN && tid < 16) {
+    tb.rl[tid] = (T)dp->op.rlin[tid];
+    tb.rl[16 + tid] = (T)dp->op.rlinb[tid];
+  }
+}
+
+// One tile t of the pass on the state (re, im).  All threads of the block;
+// sre/sim hold G * 4^K entries each.  Ends synchronised.
+template <typename T, int K, int CLS>
+__device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeader& h,
+                         const PassTables<T, K, CLS>& tb, uint64_t t, T* __restrict__ sre, T* __restrict__ sim) {
+  constexpr int D = 1 << K;
+  using T2 = typename Vec2<T>::type;
+  const int tid = threadIdx.x;
+  const int L = h.L, mhi = h.mhi, g = h.g;
+  const int G = 1 << g;
+  const int tile = G * D * D;
+  const int runlen = 1 << L;
+  const bool has_item = tid < G * D;
+  int lf = 0;
+  {
+    const int f = tid & (G - 1);
+    for (int j = 0; j < g; j++) lf |= ((f >> j) & 1) << h.freepos[j];
+  }
+  const int r_item = tid >> g;  // b in the ket step, a in the bra step
+
+  // tile base: insert zero bits at the high target positions into (t << L)
+  uint64_t base = t << L;
+  for (int j = 0; j < mhi; j++) {
+    const int p = h.hipos[j];
+    base = ((base >> p) << (p + 1)) | (base & ((1ull << p) - 1));
+  }
+  // ---- load touched runs (pairs of entries; runs are >= 2 long)
+  for (int e2 = tid; e2 < (tile >> 1); e2 += blockDim.x) {
+    const int e = e2 << 1;
+    const int run = e >> L;
+    if (!((tb.ldmask[run >> 5] >> (run & 31)) & 1)) continue;
+    const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
+    const T2 vr = *reinterpret_cast<const T2*>(re + ga);
+    const T2 vi = *reinterpret_cast<const T2*>(im + ga);
+    *reinterpret_cast<T2*>(sre + e) = vr;
+    *reinterpret_cast<T2*>(sim + e) = vi;
+  }
+  __syncthreads();
+
+  if (CLS == CLS_DENSE || CLS == CLS_SPARSE || CLS == CLS_RLIN) {
+    // ---- ket step: column (., b, f) <- U column
+    if (has_item) {
+      const int b = r_item;
+      const int cb = lf + tb.lb[b];
+      if (CLS == CLS_RLIN) {
+        const int p0 = cb + tb.lk[0], p1 = cb + tb.lk[1];
+        const T v[4] = {sre[p0], sim[p0], sre[p1], sim[p1]};
+        T o[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+          o[i] = tb.rl[4 * i] * v[0] + tb.rl[4 * i + 1] * v[1] + tb.rl[4 * i + 2] * v[2] + tb.rl[4 * i + 3] * v[3];
+        sre[p0] = o[0]; sim[p0] = o[1]; sre[p1] = o[2]; sim[p1] = o[3];
+      } else if (CLS == CLS_DENSE) {
+        T xr[D], xi[D];
+#pragma unroll
+        for (int c = 0; c < D; c++) {
+          xr[c] = sre[cb + tb.lk[c]];
+          xi[c] = sim[cb + tb.lk[c]];
+        }
+#pragma unroll
+        for (int a = 0; a < D; a++) {
+          T ar = 0, ai = 0;
+#pragma unroll
+          for (int c = 0; c < D; c++) {
+            const T ur = tb.ure[a * D + c], ui = tb.uim[a * D + c];
+            ar = fma(ur, xr[c], ar);
+            ar = fma(-ui, xi[c], ar);
+            ai = fma(ur, xi[c], ai);
+            ai = fma(ui, xr[c], ai);
+          }
+          sre[cb + tb.lk[a]] = ar;
+          sim[cb + tb.lk[a]] = ai;
+        }
+      } else {  // SPARSE
+        T yr[D], yi[D];
+#pragma unroll
+        for (int a = 0; a < D; a++) {
+          T ar = 0, ai = 0;
+          const int nz = tb.nnz[a];
+          for (int j = 0; j < nz; j++) {
+            const int c = tb.col[a * D + j];
+            const T ur = tb.ure[a * D + c], ui = tb.uim[a * D + c];
+            const T vr = sre[cb + tb.lk[c]], vi = sim[cb + tb.lk[c]];
+            ar = fma(ur, vr, ar);
+            ar = fma(-ui, vi, ar);
+            ai = fma(ur, vi, ai);
+            ai = fma(ui, vr, ai);
+          }
+          yr[a] = ar;
+          yi[a] = ai;
+        }
+#pragma unroll
+        for (int a = 0; a < D; a++) {
+          sre[cb + tb.lk[a]] = yr[a];
+          sim[cb + tb.lk[a]] = yi[a];
+        }
+      }
+    }
+    __syncthreads();
+    // ---- bra step: row (a, ., f) <- V row (V = conj(U) for a superoperator pass)
+    if (has_item) {
+      const int a = r_item;
+      const int ca = lf + tb.lk[a];
+      if (CLS == CLS_RLIN) {
+        const int p0 = ca + tb.lb[0], p1 = ca + tb.lb[1];
+        const T v[4] = {sre[p0], sim[p0], sre[p1], sim[p1]};
+        T o[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+          o[i] = tb.rl[16 + 4 * i] * v[0] + tb.rl[16 + 4 * i + 1] * v[1] + tb.rl[16 + 4 * i + 2] * v[2] +
+                 tb.rl[16 + 4 * i + 3] * v[3];
+        sre[p0] = o[0]; sim[p0] = o[1]; sre[p1] = o[2]; sim[p1] = o[3];
+      } else if (CLS == CLS_DENSE) {
+        T xr[D], xi[D];
+#pragma unroll
+        for (int c = 0; c < D; c++) {
+          xr[c] = sre[ca + tb.lb[c]];
+          xi[c] = sim[ca + tb.lb[c]];
+        }
+#pragma unroll
+        for (int b = 0; b < D; b++) {
+          T ar = 0, ai = 0;
+#pragma unroll
+          for (int c = 0; c < D; c++) {
+            const T vr = tb.vre[b * D + c], vi = tb.vim[b * D + c];
+            ar = fma(vr, xr[c], ar);
+            ar = fma(-vi, xi[c], ar);
+            ai = fma(vr, xi[c], ai);
+            ai = fma(vi, xr[c], ai);
+          }
+          sre[ca + tb.lb[b]] = ar;
+          sim[ca + tb.lb[b]] = ai;
+        }
+      } else {  // SPARSE
+        T yr[D], yi[D];
+#pragma unroll
+        for (int b = 0; b < D; b++) {
+          T ar = 0, ai = 0;
+          const int nz = tb.nnzb[b];
+          for (int j = 0; j < nz; j++) {
+            const int c = tb.colb[b * D + j];
+            const T mr = tb.vre[b * D + c], mi = tb.vim[b * D + c];
+            const T vr = sre[ca + tb.lb[c]], vi = sim[ca + tb.lb[c]];
+            ar = fma(mr, vr, ar);
+            ar = fma(-mi, vi, ar);
+            ai = fma(mr, vi, ai);
+            ai = fma(mi, vr, ai);
+          }
+          yr[b] = ar;
+          yi[b] = ai;
+        }
+#pragma unroll
+        for (int b = 0; b < D; b++) {
+          sre[ca + tb.lb[b]] = yr[b];
+          sim[ca + tb.lb[b]] = yi[b];
+        }
+      }
+    }
+    __syncthreads();
+    // ---- store touched runs
+    for (int e2 = tid; e2 < (tile >> 1); e2 += blockDim.x) {
+      const int e = e2 << 1;
+      const int run = e >> L;
+      if (!((tb.stmask[run >> 5] >> (run & 31)) & 1)) continue;
+      const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
+      *reinterpret_cast<T2*>(re + ga) = *reinterpret_cast<const T2*>(sre + e);
+      *reinterpret_cast<T2*>(im + ga) = *reinterpret_cast<const T2*>(sim + e);
+    }
+  } else {
+    // ---- monomial: out[a][b] = f[a][b] * in[src[a]][srcb[b]], fused into the store
+    for (int e2 = tid; e2 < (tile >> 1); e2 += blockDim.x) {
+      const int e = e2 << 1;
+      const int run = e >> L;
+      if (!((tb.stmask[run >> 5] >> (run & 31)) & 1)) continue;
+      T outr[2], outi[2];
+#pragma unroll
+      for (int u = 0; u < 2; u++) {
+        const int loc = e + u;
+        const int a = pext_local<K>(loc, tb.lket);
+        const int b = pext_local<K>(loc, tb.lbra);
+        const int sa = tb.src[a], sb = tb.srcb[b];
+        const int sl = loc - tb.lk[a] - tb.lb[b] + tb.lk[sa] + tb.lb[sb];
+        const T vr = sre[sl], vi = sim[sl];
+        if (CLS == CLS_MOVE) {
+          outr[u] = vr;
+          outi[u] = vi;
+        } else {
+          const int fk = tb.fk[a * D + b];
+          if (CLS == CLS_PHASE && fk == FK_GEN) {
+            const T fr = tb.fre[a * D + b], fi = tb.fim[a * D + b];
+            outr[u] = fma(fr, vr, -fi * vi);
+            outi[u] = fma(fr, vi, fi * vr);
+          } else if (fk == FK_ONE) {
+            outr[u] = vr;
+            outi[u] = vi;
+          } else if (fk == FK_NEG) {
+            outr[u] = flip(vr);
+            outi[u] = flip(vi);
+          } else if (fk == FK_PI) {  // i*(vr + i vi) = -vi + i vr
+            outr[u] = flip(vi);
+            outi[u] = vr;
+          } else {  // -i*(vr + i vi) = vi - i vr
+            outr[u] = vi;
+            outi[u] = flip(vr);
+          }
+        }
+      }
+      const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
+      T2 wr, wi;
+      wr.x = outr[0];
+      wr.y = outr[1];
+      wi.x = outi[0];
+      wi.y = outi[1];
+      *reinterpret_cast<T2*>(re + ga) = wr;
+      *reinterpret_cast<T2*>(im + ga) = wi;
+    }
+  }
+  __syncthreads();
+}
+
+}  // namespace dmg

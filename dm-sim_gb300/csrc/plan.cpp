@@ -113,7 +113,30 @@ std::vector<PassSpec> plan_reference_order(const std::vector<Basic>& basics) {
   return out;
 }
 
-std::vector<PassSpec> plan_greedy(const std::vector<Basic>& basics, int maxk) {
+namespace {
+// max nonzeros in a row of the D x D matrix U (entries below 1e-13 count as zero)
+int max_row_nnz(const cplx* U, int D) {
+  int mx = 0;
+  for (int a = 0; a < D; a++) {
+    int r = 0;
+    for (int c = 0; c < D; c++) r += std::abs(U[a * D + c]) > 1e-13;
+    mx = std::max(mx, r);
+  }
+  return mx;
+}
+// U (over K qubits) -> U (x) I on one more qubit (the new highest sub-index bit)
+void widen(cplx* U, int K) {
+  const int D = 1 << K, D2 = 2 * D;
+  cplx T[kMaxD * kMaxD];
+  for (int i = 0; i < D2 * D2; i++) T[i] = 0;
+  for (int x = 0; x < 2; x++)
+    for (int a = 0; a < D; a++)
+      for (int c = 0; c < D; c++) T[(a + D * x) * D2 + (c + D * x)] = U[a * D + c];
+  std::memcpy(U, T, sizeof(cplx) * D2 * D2);
+}
+}  // namespace
+
+std::vector<PassSpec> plan_greedy(const std::vector<Basic>& basics, int maxk, int row_cap) {
   std::vector<PassSpec> out;
   const int m = (int)basics.size();
   if (maxk < 1) maxk = 1;
@@ -141,70 +164,72 @@ std::vector<PassSpec> plan_greedy(const std::vector<Basic>& basics, int maxk) {
   };
   const int kWindow = 96;  // look-ahead over untaken gates
   int first = 0;
+  std::vector<int> cand;
   while (first < m) {
     while (first < m && taken[first]) first++;
     if (first >= m) break;
     const Basic& b0 = basics[first];
-    if (b0.kind == BK_RLIN) {  // real-linear gates are fusion barriers
+    if (b0.kind == BK_RLIN || nq(b0) > maxk) {  // real-linear gates are fusion barriers
       take(first);
       out.push_back(single(b0));
       continue;
     }
-    int qs[kMaxK];
-    int K = 0;
-    qs[K++] = b0.q[0];
-    if (nq(b0) == 2) qs[K++] = b0.q[1];
-    if (K > maxk) {  // a 2-qubit gate with maxk == 1: its own pass
-      take(first);
-      out.push_back(single(b0));
-      continue;
-    }
-    std::vector<int> members{first};
+    PassSpec p;
+    p.K = 0;
+    p.U[0] = 1.0;
+    auto add_qubit = [&](PassSpec& ps, int q) {
+      for (int i = 0; i < ps.K; i++)
+        if (ps.q[i] == q) return;
+      widen(ps.U, ps.K);
+      ps.q[ps.K++] = q;
+    };
+    add_qubit(p, b0.q[0]);
+    if (nq(b0) == 2) add_qubit(p, b0.q[1]);
+    apply_basic(p.U, p.K, p.q, b0);
     take(first);
+    int members = 1;
     for (;;) {
-      int best = -1, best_new = 99;
+      // candidates in preference order: fewest new qubits, then program order
+      cand.clear();
       int seen = 0;
       for (int j = first + 1; j < m && seen < kWindow; j++) {
         if (taken[j]) continue;
         seen++;
         const Basic& b = basics[j];
-        if (b.kind == BK_RLIN) continue;
-        if (!is_front(j)) continue;
+        if (b.kind == BK_RLIN || !is_front(j)) continue;
         int add = 0;
-        const int bq[2] = {b.q[0], b.q[1]};
         for (int t = 0; t < nq(b); t++) {
           bool in = false;
-          for (int i = 0; i < K; i++) in |= qs[i] == bq[t];
+          for (int i = 0; i < p.K; i++) in |= p.q[i] == b.q[t];
           add += in ? 0 : 1;
         }
-        if (K + add > maxk) continue;
-        if (add < best_new) {
-          best_new = add;
-          best = j;
-          if (add == 0) break;
-        }
+        if (p.K + add > maxk) continue;
+        cand.push_back(add * m + j);
       }
-      if (best < 0) break;
-      const Basic& b = basics[best];
-      for (int t = 0; t < nq(b); t++) {
-        bool in = false;
-        for (int i = 0; i < K; i++) in |= qs[i] == b.q[t];
-        if (!in) qs[K++] = b.q[t];
+      if (cand.empty()) break;
+      std::sort(cand.begin(), cand.end());
+      bool grown = false;
+      for (int key : cand) {
+        const int j = key % m;
+        PassSpec trial = p;
+        const Basic& b = basics[j];
+        add_qubit(trial, b.q[0]);
+        if (nq(b) == 2) add_qubit(trial, b.q[1]);
+        apply_basic(trial.U, trial.K, trial.q, b);
+        if (row_cap < kMaxD && max_row_nnz(trial.U, 1 << trial.K) > row_cap) continue;
+        p = trial;
+        take(j);
+        members++;
+        grown = true;
+        break;
       }
-      members.push_back(best);
-      take(best);
+      if (!grown) break;
     }
-    if (members.size() == 1) {
-      out.push_back(single(basics[members[0]]));
+    if (members == 1) {
+      out.push_back(single(b0));
       continue;
     }
-    PassSpec p;
-    p.K = K;
-    for (int i = 0; i < K; i++) p.q[i] = qs[i];
-    const int D = 1 << K;
-    for (int i = 0; i < D * D; i++) p.U[i] = (i / D == i % D) ? cplx(1, 0) : cplx(0, 0);
-    for (int j : members) apply_basic(p.U, K, qs, basics[j]);
-    p.nbasic = (int)members.size();
+    p.nbasic = members;
     classify(p, true);
     out.push_back(p);
   }

@@ -39,7 +39,9 @@ struct PassFeatures {
 //   greedy: grow each pass with the earliest ready gate that keeps the width <= maxk
 //   (prefer gates inside the current qubit set), the fixed-width planner.
 std::vector<PassSpec> plan_plain(const std::vector<Basic>& basics);
-std::vector<PassSpec> plan_greedy(const std::vector<Basic>& basics, int maxk);
+//   row_cap: a candidate gate is not absorbed if the fused operator would get
+//   more than row_cap nonzeros in a row (kMaxD = no cap).
+std::vector<PassSpec> plan_greedy(const std::vector<Basic>& basics, int maxk, int row_cap = kMaxD);
 // The reference's own order for circuits holding a real-linear gate (SRN):
 // every gate on the ket bits only, the conjugate transpose, every gate again
 // (src/dmsim_nvgpu_omp.cuh:918-969).  For complex-linear circuits and a

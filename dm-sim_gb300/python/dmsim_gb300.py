@@ -73,6 +73,15 @@ def lib():
         "dmsim_compare_states": [H, H, P(d)],
         "dmsim_alloc_host": [ctypes.c_size_t, P(ctypes.c_void_p)],
         "dmsim_free_host": [ctypes.c_void_p],
+        "dmsim_cost_collect": [u32, u32, u32, u64, P(d), P(d), u32, P(u32)],
+        "dmsim_cost_train": [P(d), P(d), u32, u32, d, u64, P(d)],
+        "dmsim_cost_predict": [P(d), u32, P(d)],
+        "dmsim_cost_save": [ctypes.c_char_p],
+        "dmsim_cost_load": [ctypes.c_char_p],
+        "dmsim_mlp_forward": [P(ctypes.c_float), P(ctypes.c_float), u32, P(ctypes.c_float)],
+        "dmsim_mlp_grad": [P(ctypes.c_float), P(ctypes.c_float), P(ctypes.c_float), u32, P(ctypes.c_float),
+                           P(ctypes.c_float)],
+        "dmsim_plan_predicted_ms": [H, P(d)],
         "dmsim_plan_inspect": [u32, P(ctypes.c_int32), P(u32), P(d), P(d), u32, ctypes.c_int, ctypes.c_int,
                                ctypes.c_int, P(d), u32, P(u32)],
     }
@@ -264,6 +273,11 @@ class Simulation:
         """Copy rho into caller-provided float64 buffers (e.g. PinnedBuffer arrays)."""
         self._check(lib().dmsim_get_dm(self._h, _dp(re), _dp(im)))
 
+    def predicted_ms(self):
+        v = ctypes.c_double()
+        self._check(lib().dmsim_plan_predicted_ms(self._h, ctypes.byref(v)))
+        return v.value
+
     def device_state(self):
         re, im = ctypes.c_void_p(), ctypes.c_void_p()
         self._check(lib().dmsim_device_state(self._h, ctypes.byref(re), ctypes.byref(im)))
@@ -345,3 +359,69 @@ class PinnedBuffer:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------- cost model
+COST_FEATURES = 16
+MLP_PARAMS = 1633
+
+
+def _fp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _ok(st, what):
+    if st != OK:
+        raise DMSimError(st, f"{what}: {lib().dmsim_status_string(st).decode()}")
+
+
+def cost_collect(n, n_circuits=2, gates=60, seed=0, cap=200000):
+    """Per-pass (features, ms) samples the engine records on its own random
+    circuits under several fusion plans, timed with CUDA events on the GPU."""
+    feats = np.zeros((cap, COST_FEATURES))
+    ms = np.zeros(cap)
+    cnt = ctypes.c_uint32()
+    _ok(lib().dmsim_cost_collect(n, n_circuits, gates, seed, _dp(feats), _dp(ms), cap, ctypes.byref(cnt)), "cost_collect")
+    k = min(cnt.value, cap)
+    return feats[:k].copy(), ms[:k].copy()
+
+
+def cost_train(feats, ms, steps=3000, lr=3e-3, seed=1):
+    feats = np.ascontiguousarray(feats, dtype=np.float64)
+    ms = np.ascontiguousarray(ms, dtype=np.float64)
+    loss = np.zeros(2)
+    _ok(lib().dmsim_cost_train(_dp(feats), _dp(ms), len(ms), steps, lr, seed, _dp(loss)), "cost_train")
+    return loss
+
+
+def cost_predict(feats):
+    feats = np.ascontiguousarray(feats, dtype=np.float64)
+    out = np.zeros(len(feats))
+    _ok(lib().dmsim_cost_predict(_dp(feats), len(feats), _dp(out)), "cost_predict")
+    return out
+
+
+def cost_save(path):
+    _ok(lib().dmsim_cost_save(path.encode()), "cost_save")
+
+
+def cost_load(path):
+    _ok(lib().dmsim_cost_load(path.encode()), "cost_load")
+
+
+def mlp_forward(params, X):
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    y = np.zeros(len(X), dtype=np.float32)
+    _ok(lib().dmsim_mlp_forward(_fp(params), _fp(X), len(X), _fp(y)), "mlp_forward")
+    return y
+
+
+def mlp_grad(params, X, T):
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    T = np.ascontiguousarray(T, dtype=np.float32)
+    g = np.zeros(MLP_PARAMS, dtype=np.float32)
+    loss = np.zeros(1, dtype=np.float32)
+    _ok(lib().dmsim_mlp_grad(_fp(params), _fp(X), _fp(T), len(X), _fp(g), _fp(loss)), "mlp_grad")
+    return g, float(loss[0])

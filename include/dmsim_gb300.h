@@ -125,6 +125,31 @@ int dmsim_free_host(void* p);
 int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qubits, const double* params,
                        const double* mats, uint32_t ngates, int mode, int max_k, int planner,
                        double* out, uint32_t cap, uint32_t* npasses);
+/* ---- learned pass-time model (process-wide) --------------------------------
+ * Features: DMSIM_COST_FEATURES doubles per pass (width, class, density,
+ * touched fractions, target-bit positions, size, precision).
+ * dmsim_cost_collect: run the engine's own random circuits (29-entry mixed
+ * table, n qubits, mt19937_64 from seed) under several fusion plans on the
+ * current GPU, timing every pass with CUDA events; writes up to cap samples
+ * and the total count.  dmsim_cost_train: fit the network on the GPU (Adam,
+ * full batch, steps, lr, weights seeded by seed); loss[0..1] = first / last
+ * mean squared error of standardised log time.  dmsim_cost_predict: GPU
+ * inference, ms per sample.  save / load: the weights file. */
+#define DMSIM_COST_FEATURES 16
+int dmsim_cost_collect(uint32_t n, uint32_t n_circuits, uint32_t gates, uint64_t seed, double* feats, double* ms,
+                       uint32_t cap, uint32_t* count);
+int dmsim_cost_train(const double* feats, const double* ms, uint32_t count, uint32_t steps, double lr, uint64_t seed,
+                     double loss[2]);
+int dmsim_cost_predict(const double* feats, uint32_t count, double* out_ms);
+int dmsim_cost_save(const char* path);
+int dmsim_cost_load(const char* path);
+/* The network's forward pass and its loss gradient on the GPU for given
+ * parameters (DMSIM_MLP_PARAMS floats) -- the hooks the gradient check uses. */
+#define DMSIM_MLP_PARAMS 1633
+int dmsim_mlp_forward(const float* params, const float* X, uint32_t B, float* y);
+int dmsim_mlp_grad(const float* params, const float* X, const float* T, uint32_t B, float* grad, float* loss);
+/* Predicted run time of the uploaded plan (learned planner), ms */
+int dmsim_plan_predicted_ms(dmsim_handle h, double* ms);
 /* Device pointers of rho (for in-HBM benchmarks and interop) */
 int dmsim_device_state(dmsim_handle h, void** re, void** im);
 const char* dmsim_last_error(dmsim_handle h);

@@ -64,6 +64,19 @@ def test_random_circuits(engine, oracle, mode, max_k, n, seed):
     assert maxerr(got, ref) <= (1e-12 if mode == "plain" else 1e-10)
 
 
+@pytest.mark.parametrize("mode", ["plain", "fused"])
+def test_srn_circuits_reference_order(engine, oracle, mode):
+    """All 38 gates, SRN included: a circuit with SRN runs in the reference's
+    own forward / conjugate-transpose / forward order and matches it."""
+    n = 6
+    for seed in range(2):
+        circ = W.random_circuit(n, 60, seed=600 + seed)
+        circ.insert(3, (W.OP["SRN"], (seed,), 0.0, 0.0, 0.0))
+        ref = oracle.dm_sim(n, circ)
+        got = run_engine(engine, n, circ, mode)
+        assert maxerr(got, ref) <= 1e-12
+
+
 def test_c1_c2(engine, oracle):
     rng = np.random.default_rng(8)
 

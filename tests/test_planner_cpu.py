@@ -95,12 +95,15 @@ def test_plain_classes(engine):
     """Each basic gate lands in the class its structure allows."""
     n = 3
     cases = {"X": "MOVE", "CX": "MOVE", "Y": "SIGNED", "Z": "SIGNED", "S": "SIGNED", "SDG": "SIGNED",
-             "T": "PHASE", "TDG": "PHASE", "U1": "PHASE", "H": "DENSE", "U3": "DENSE", "SRN": "RLIN"}
+             "T": "PHASE", "TDG": "PHASE", "U1": "PHASE", "H": "DENSE", "U3": "DENSE"}
     for name, cls in cases.items():
         op = W.OP[name]
         qs = (0, 1) if W.ARITY[op] == 2 else (1,)
         p = engine.plan_inspect(n, [(op, qs, 0.3, 0.2, 0.1)], mode="plain")
         assert [x["cls"] for x in p] == [cls], name
+    # SRN: the reference's order, ket-only passes around the adjoint stage
+    p = engine.plan_inspect(n, [(W.OP["SRN"], (1,), 0, 0, 0)], mode="plain")
+    assert [x["cls"] for x in p] == ["RLIN", "TRANSPOSE", "RLIN"] and p[0]["ket_only"]
 
 
 def test_fused_toffoli_is_pure_data_movement(engine):
