@@ -716,6 +716,31 @@ int dmsim_free_host(void* p) {
   return cudaFreeHost(p) == cudaSuccess ? DMSIM_OK : DMSIM_ERR_CUDA;
 }
 
+int dmsim_pure_metrics_noalloc(dmsim_handle s, const double* psi_re, const double* psi_im, double out[4]) {
+  if (!s) return DMSIM_ERR_ARG;
+  if (!psi_re || !psi_im || !out) {
+    s->err = "dmsim_pure_metrics_noalloc: null argument";
+    return DMSIM_ERR_ARG;
+  }
+  if (s->n > (uint32_t)kNoAllocMaxQubits) {
+    s->err = "dmsim_pure_metrics_noalloc: the state has more than 16 qubits, beyond its static scratch of 2^16 "
+             "amplitudes; use dmsim_pure_metrics";
+    return DMSIM_ERR_ARG;
+  }
+  if (!s->d_re) {  // allocating rho here would defeat the purpose
+    s->err = "dmsim_pure_metrics_noalloc: rho is not allocated yet";
+    return DMSIM_ERR_STATE;
+  }
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e == cudaSuccess) e = pure_metrics_noalloc(s->d_re, s->d_im, s->fp32, psi_re, psi_im, (int)s->n, s->sms, s->stream, out);
+  if (e != cudaSuccess) {
+    s->err = std::string("dmsim_pure_metrics_noalloc: ") + cudaGetErrorString(e);
+    return DMSIM_ERR_CUDA;
+  }
+  s->err.clear();
+  return DMSIM_OK;
+}
+
 int dmsim_device_state(dmsim_handle s, void** re, void** im) {
   DM_TRY(s, {
     ensure_state(s);

@@ -8,9 +8,19 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+#include <mutex>
+
 #include "metrics.h"
 
 namespace dmg {
+
+// Scratch of the no-allocation metrics entry point (dmsim_pure_metrics_noalloc):
+// the pure state's real parts, its imaginary parts (kNoAllocMaxDim each) and
+// four accumulators -- 1 MiB + 64 B, held by every GPU that loads the library
+// until the process exits.  Host code must not use this name as a device
+// address; it asks the runtime for the address (noalloc_scratch below).
+static __device__ __align__(256) double g_noalloc_scratch[2 * kNoAllocMaxDim + 8];
 
 __device__ __forceinline__ void atomic_max_nonneg(double* addr, double v) {
   // non-negative doubles order like their bit patterns
@@ -112,6 +122,54 @@ cudaError_t launch_pure_metrics(const void* re, const void* im, bool fp32, const
   else
     k_pure_metrics<double><<<grid, 256, 0, s>>>((const double*)re, (const double*)im, psi_re, psi_im, n, d_acc);
   return cudaGetLastError();
+}
+
+namespace {
+std::mutex g_noalloc_mu;
+double* g_noalloc_addr[256] = {};  // device address of the scratch, per device ordinal
+}  // namespace
+
+// Once per device, with that device current: look up the scratch's device
+// address.  Later calls on the device reuse it.
+static cudaError_t noalloc_scratch(double** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_addr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_addr[dev];
+  return cudaSuccess;
+}
+
+cudaError_t pure_metrics_noalloc(const void* re, const void* im, bool fp32, const double* psi_re, const double* psi_im,
+                                 int n, int sms, cudaStream_t s, double out[4]) {
+  if (n < 1 || n > kNoAllocMaxQubits) return cudaErrorInvalidValue;
+  double* scratch = nullptr;
+  cudaError_t e = noalloc_scratch(&scratch);
+  if (e != cudaSuccess) return e;
+  const size_t dim = (size_t)1 << n;
+  double* d_pr = scratch;
+  double* d_pi = scratch + kNoAllocMaxDim;
+  double* d_acc = scratch + 2 * kNoAllocMaxDim;
+  e = cudaMemcpyAsync(d_pr, psi_re, dim * sizeof(double), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_pi, psi_im, dim * sizeof(double), cudaMemcpyHostToDevice, s);
+  // launch_pure_metrics zeroes the accumulators before the kernel
+  if (e == cudaSuccess) e = launch_pure_metrics(re, im, fp32, d_pr, d_pi, n, d_acc, sms, s);
+  double acc[4] = {0, 0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(acc, d_acc, 4 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return e;
+  out[0] = acc[0];
+  out[1] = acc[1];
+  out[2] = std::sqrt(acc[2]);
+  out[3] = std::sqrt(acc[3]);
+  return cudaSuccess;
 }
 
 }  // namespace dmg

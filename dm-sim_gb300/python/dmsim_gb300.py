@@ -69,6 +69,7 @@ def lib():
         "dmsim_last_timings": [H, P(d)],
         "dmsim_pass_records": [H, P(d), u32, P(u32)],
         "dmsim_pure_metrics": [H, P(d), P(d), P(d)],
+        "dmsim_pure_metrics_noalloc": [H, P(d), P(d), P(d)],
         "dmsim_device_state": [H, P(ctypes.c_void_p), P(ctypes.c_void_p)],
         "dmsim_compare_states": [H, H, P(d)],
         "dmsim_alloc_host": [ctypes.c_size_t, P(ctypes.c_void_p)],

@@ -106,6 +106,20 @@ int dmsim_pass_records(dmsim_handle h, double* out, uint32_t cap, uint32_t* coun
  * out[0] = fidelity <psi|rho|psi>, out[1] = trace, out[2] = max |rho - psi psi^+|,
  * out[3] = ||rho - psi psi^+||_F. */
 int dmsim_pure_metrics(dmsim_handle h, const double* psi_re, const double* psi_im, double out[4]);
+/* dmsim_pure_metrics without any allocation.  No counterpart in the reference.
+ * For callers that cannot call cudaMalloc: processes whose device memory is
+ * already reserved by another allocator (a framework's caching pool), and
+ * monitoring loops that must not stall running work on cudaMalloc/cudaFree's
+ * implicit synchronisation.  psi is staged in a 1 MiB array fixed in the
+ * library's device image (every GPU that loads the library holds it until the
+ * process exits), so states are limited to 16 qubits (2^16 amplitudes); larger
+ * states get DMSIM_ERR_ARG with a message.  The first call on a device looks
+ * up the array's address on that device: make it before any stream capture.
+ * Every call reuses the same array (the accumulators are cleared each call,
+ * psi is overwritten), so calls that overlap on the GPU -- from two threads or
+ * two handles on the same device -- race; serialise them.  Same outputs as
+ * dmsim_pure_metrics; rho must already be allocated (DMSIM_ERR_STATE if not). */
+int dmsim_pure_metrics_noalloc(dmsim_handle h, const double* psi_re, const double* psi_im, double out[4]);
 /* Compare two states of the same size and precision on the device:
  * out[0] = max |A - B| over entries, out[1] = ||A - B||_F. */
 int dmsim_compare_states(dmsim_handle a, dmsim_handle b, double out[2]);
