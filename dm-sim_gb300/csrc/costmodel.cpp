@@ -13,7 +13,7 @@
 
 namespace dmg {
 
-void pass_features(const PassFeatures& f, bool fp32, float* x) {
+void pass_features(const PassFeatures& f, float* x) {
   const double nb = 2.0 * f.n;
   for (int i = 0; i < kMlpIn; i++) x[i] = 0.f;
   x[0] = f.K / 4.0f;
@@ -26,7 +26,7 @@ void pass_features(const PassFeatures& f, bool fp32, float* x) {
   x[11] = (float)((f.max_lo_bit + 1) / nb);
   x[12] = (float)(f.min_hi_bit / nb);
   x[13] = (float)(nb / 34.0);                     // log2 of the entry count
-  x[14] = fp32 ? 1.f : 0.f;
+  x[14] = f.arith == 1 ? 1.f : (f.arith == 2 ? 0.5f : 0.f);  // FP32 / double-float / FP64
   x[15] = (float)((f.nnz / (double)D) * f.ld_frac * std::ldexp(1.0, (int)nb - 28));  // arithmetic volume
 }
 
@@ -201,7 +201,7 @@ bool cost_model_predict(const CostModel& m, const std::vector<float>& X, std::ve
   return true;
 }
 
-std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int maxk, bool fp32, const CostModel& m,
+std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int maxk, int arith, const CostModel& m,
                                    double* predicted_ms, std::string& err) {
   // candidate plans: the unfused plan, and greedy plans of every width up to
   // maxk under row-density caps
@@ -223,8 +223,9 @@ std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int 
       std::memset(&f, 0, sizeof f);
       if (p.transpose) continue;
       build_desc(p, n, buf.data(), &f, nullptr, nullptr);
+      f.arith = arith;
       float x[kMlpIn];
-      pass_features(f, fp32, x);
+      pass_features(f, x);
       X.insert(X.end(), x, x + kMlpIn);
       owner.push_back((int)c);
     }

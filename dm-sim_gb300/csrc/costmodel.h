@@ -11,7 +11,7 @@
 namespace dmg {
 
 // Features of one pass for the cost model (kMlpIn floats, roughly in [0,1]).
-void pass_features(const PassFeatures& f, bool fp32, float* out);
+void pass_features(const PassFeatures& f, float* out);
 
 struct CostModel {
   bool ready = false;
@@ -34,7 +34,8 @@ bool cost_model_predict(const CostModel& m, const std::vector<float>& X, std::ve
 
 // The learned planner: scores candidate plans (widths 1..maxk, row-density
 // caps, and the unfused plan) with the model, returns the cheapest.
-std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int maxk, bool fp32, const CostModel& m,
+// arith: the arithmetic the chosen plan will run in (kernels.h Arith).
+std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int maxk, int arith, const CostModel& m,
                                    double* predicted_ms, std::string& err);
 
 }  // namespace dmg

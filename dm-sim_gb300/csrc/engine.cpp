@@ -70,6 +70,8 @@ struct dmsim_sim {
   cudaGraphExec_t gexec = nullptr;
 
   int mode = 0, maxk = 4, planner = 0, record = 0, graph_on = 1, verbose = 0;
+  int fused_arith = 1;  // fused FP64 runs compute in double-float (1) or FP64 (0)
+  int arith = 0;        // arithmetic of the uploaded plan (kernels.h Arith)
   int64_t seed = -1;
 
   double last_ms = 0, last_bytes = 0, predicted_ms = 0;
@@ -133,6 +135,13 @@ void check_qubits(const dmsim_sim* s, const GateRec& g) {
 void enqueue_passes(dmsim_sim* s, bool timed) {
   for (size_t i = 0; i < s->passes.size(); i++) {
     PassInfo& p = s->passes[i];
+    if (p.conv) {
+      if (timed) DM_CUDA(cudaEventRecord(p.ev0, s->stream));
+      if (p.conv == 1) DM_CUDA(launch_to_df64(s->d_re, s->d_im, s->N, p.grid, s->stream));
+      else DM_CUDA(launch_from_df64(s->d_re, s->d_im, s->N, p.grid, s->stream));
+      if (timed) DM_CUDA(cudaEventRecord(p.ev1, s->stream));
+      continue;
+    }
     if (p.transpose) {
       if (timed) DM_CUDA(cudaEventRecord(p.ev0, s->stream));
       DM_CUDA(launch_conj_transpose(s->d_re, s->d_im, (int)s->n, s->fp32, p.grid, s->stream));
@@ -146,6 +155,7 @@ void enqueue_passes(dmsim_sim* s, bool timed) {
     a.K = p.K;
     a.cls = p.cls;
     a.fp32 = s->fp32;
+    a.arith = s->arith;
     a.grid = p.grid;
     a.tile_entries = p.tile_entries;
     if (timed) DM_CUDA(cudaEventRecord(p.ev0, s->stream));
@@ -170,6 +180,15 @@ void load_default_cost_model() {
   if (!path.empty()) cost_model_load(global_cost_model(), path);
 }
 
+// Arithmetic of a run: complex64 state -> FP32; a fused FP64 run ->
+// double-float unless the option asks for FP64; otherwise (the plain path, the
+// reference's order for SRN) FP64.
+int run_arith(const dmsim_sim* s, bool reference_order) {
+  if (s->fp32) return AR_FP32;
+  if (s->mode == 1 && s->fused_arith && !reference_order) return AR_DF64;
+  return AR_FP64;
+}
+
 // Plain: one pass per basic gate.  Fused: the greedy (fixed-width) or the
 // learned planner.  A circuit holding a real-linear gate (SRN) runs in the
 // reference's own order in either mode, the only order that reproduces it.
@@ -185,27 +204,30 @@ std::vector<PassSpec> make_plan(dmsim_sim* s, const std::vector<Basic>& basics) 
       throw DmError{DMSIM_ERR_STATE, "the learned planner needs a cost model: train one (dmsim_cost_train) or load one "
                                      "(dmsim_cost_load, or set DMSIM_COST_MODEL)"};
     std::string err;
-    std::vector<PassSpec> p = plan_learned(basics, (int)s->n, s->maxk, s->fp32, m, &s->predicted_ms, err);
+    std::vector<PassSpec> p = plan_learned(basics, (int)s->n, s->maxk, run_arith(s, false), m, &s->predicted_ms, err);
     if (!err.empty()) throw DmError{DMSIM_ERR_CUDA, "learned planner: " + err};
     return p;
   }
   return plan_greedy(basics, s->maxk);
 }
 
-void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_basic);
+void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_basic, int arith);
 
 void upload(dmsim_sim* s) {
   if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "upload() called twice without clear_circuit() (:347-350)"};
   ensure_state(s);
   std::vector<Basic> basics;
   for (const GateRec& g : s->circuit) decompose(g, basics);
-  upload_specs(s, make_plan(s, basics), (uint32_t)basics.size());
+  bool rlin = false;
+  for (const Basic& b : basics) rlin |= b.kind == BK_RLIN;
+  upload_specs(s, make_plan(s, basics), (uint32_t)basics.size(), run_arith(s, rlin));
 }
 
 // Write the descriptors of a plan to the device and capture its launches.
-void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_basic) {
+void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_basic, int arith) {
   ensure_state(s);
   s->n_basic = n_basic;
+  s->arith = arith;
   // descriptors, 256-byte aligned, one host blob, one copy
   std::vector<size_t> offs;
   size_t total = 0;
@@ -215,6 +237,15 @@ void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_b
   }
   std::vector<unsigned char> blob(std::max<size_t>(total, 256));
   s->passes.clear();
+  const double conv_bytes = 2.0 * 2.0 * (double)s->N * 8.0;
+  if (arith == AR_DF64) {
+    PassInfo pi;
+    std::memset(&pi, 0, sizeof pi);
+    pi.conv = 1;
+    pi.grid = (unsigned)s->sms * 8;
+    pi.bytes = conv_bytes;
+    s->passes.push_back(pi);
+  }
   for (size_t i = 0; i < specs.size(); i++) {
     PassInfo pi;
     std::memset(&pi, 0, sizeof pi);
@@ -235,9 +266,18 @@ void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_b
     pi.tile_entries = tile;
     pi.bytes = (double)entries * 2.0 * (double)esize(s);
     pi.nbasic = specs[i].nbasic;
-    const int bps = pass_blocks_per_sm(pi.K, pi.cls, s->fp32);
+    pi.feat.arith = arith;
+    const int bps = pass_blocks_per_sm(pi.K, pi.cls, arith);
     const uint64_t cap = (uint64_t)s->sms * (uint64_t)bps;
     pi.grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, cap));
+    s->passes.push_back(pi);
+  }
+  if (arith == AR_DF64) {
+    PassInfo pi;
+    std::memset(&pi, 0, sizeof pi);
+    pi.conv = 2;
+    pi.grid = (unsigned)s->sms * 8;
+    pi.bytes = conv_bytes;
     s->passes.push_back(pi);
   }
   if (total > 0) {
@@ -444,6 +484,10 @@ int dmsim_set_option(dmsim_handle s, int key, int64_t v) {
         s->graph_on = v != 0;
         break;
       case DMSIM_OPT_VERBOSE: s->verbose = v != 0; break;
+      case DMSIM_OPT_FUSED_ARITH:
+        if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set the fused arithmetic before upload()"};
+        s->fused_arith = v != 0;
+        break;
       default: throw DmError{DMSIM_ERR_ARG, "unknown option"};
     }
   });
@@ -461,6 +505,7 @@ int dmsim_get_option(dmsim_handle s, int key, int64_t* v) {
       case DMSIM_OPT_SEED: *v = s->seed; break;
       case DMSIM_OPT_GRAPH: *v = s->graph_on; break;
       case DMSIM_OPT_VERBOSE: *v = s->verbose; break;
+      case DMSIM_OPT_FUSED_ARITH: *v = s->fused_arith; break;
       default: throw DmError{DMSIM_ERR_ARG, "unknown option"};
     }
   });
@@ -780,7 +825,7 @@ int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qu
       if (!m.ready) load_default_cost_model();
       if (!m.ready) return DMSIM_ERR_STATE;
       std::string err;
-      specs = plan_learned(basics, (int)n_qubits, max_k, false, m, nullptr, err);
+      specs = plan_learned(basics, (int)n_qubits, max_k, AR_DF64, m, nullptr, err);
       if (!err.empty()) return DMSIM_ERR_CUDA;
     } else specs = plan_greedy(basics, max_k);
     if (npasses) *npasses = (uint32_t)specs.size();
@@ -842,9 +887,9 @@ void random_table_circuit(uint32_t n, uint32_t ngates, std::mt19937_64& rng, std
 }
 }  // namespace
 
-int dmsim_cost_collect(uint32_t n, uint32_t n_circuits, uint32_t gates, uint64_t seed, double* feats, double* ms,
-                       uint32_t cap, uint32_t* count) {
-  if (!count || n < 2 || n > 16) return DMSIM_ERR_ARG;
+int dmsim_cost_collect(uint32_t n, uint32_t n_circuits, uint32_t gates, uint64_t seed, int arith, double* feats,
+                       double* ms, uint32_t cap, uint32_t* count) {
+  if (!count || n < 2 || n > 16 || arith < AR_FP64 || arith > AR_DF64 || arith == AR_FP32) return DMSIM_ERR_ARG;
   *count = 0;
   dmsim_handle h = nullptr;
   int st = dmsim_create(n, 1, &h);
@@ -865,13 +910,14 @@ int dmsim_cost_collect(uint32_t n, uint32_t n_circuits, uint32_t gates, uint64_t
         for (int rc : caps) {
           if (rc != kMaxD && rc >= (1 << k)) continue;
           std::vector<PassSpec> specs = k == 1 ? plan_plain(basics) : plan_greedy(basics, k, rc);
-          upload_specs(h, specs, (uint32_t)basics.size());
+          upload_specs(h, specs, (uint32_t)basics.size(), arith);
           h->uploaded = true;
           run(h);
           for (const PassRecord& r : h->records) {
+            if (r.feat.K == 0) continue;  // format conversions are not passes
             if (got < cap && feats && ms) {
               float x[kMlpIn];
-              pass_features(r.feat, h->fp32, x);
+              pass_features(r.feat, x);
               for (int i = 0; i < kMlpIn; i++) feats[(size_t)got * kMlpIn + i] = x[i];
               ms[got] = r.ms;
             }

@@ -80,6 +80,7 @@ static cudaError_t launch_t(const LaunchArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_pass(const LaunchArgs& a, cudaStream_t s) {
+  if (a.arith == AR_DF64) return launch_t<df64>(a, s);
   return a.fp32 ? launch_t<float>(a, s) : launch_t<double>(a, s);
 }
 
@@ -105,11 +106,41 @@ static int occ_k(int cls) {
   }
 }
 
-int pass_blocks_per_sm(int K, int cls, bool fp32) {
-  if (fp32) {
+int pass_blocks_per_sm(int K, int cls, int arith) {
+  if (arith == AR_FP32) {
     switch (K) { case 1: return occ_k<float, 1>(cls); case 2: return occ_k<float, 2>(cls); case 3: return occ_k<float, 3>(cls); default: return occ_k<float, 4>(cls); }
   }
+  if (arith == AR_DF64) {
+    switch (K) { case 1: return occ_k<df64, 1>(cls); case 2: return occ_k<df64, 2>(cls); case 3: return occ_k<df64, 3>(cls); default: return occ_k<df64, 4>(cls); }
+  }
   switch (K) { case 1: return occ_k<double, 1>(cls); case 2: return occ_k<double, 2>(cls); case 3: return occ_k<double, 3>(cls); default: return occ_k<double, 4>(cls); }
+}
+
+// ---------------------------------------------------------------- df64 format
+// In place, once per fused run: each FP64 entry becomes the double-float pair
+// (hi, lo) = (round(x), round(x - hi)) in the same 8 bytes, and back.  These
+// run on the FP64 pipe, but only twice per run.
+__global__ void k_to_df64(double* __restrict__ re, double* __restrict__ im, uint64_t N) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < N; i += (uint64_t)gridDim.x * blockDim.x) {
+    const df64 a(re[i]), b(im[i]);
+    reinterpret_cast<df64*>(re)[i] = a;
+    reinterpret_cast<df64*>(im)[i] = b;
+  }
+}
+__global__ void k_from_df64(double* __restrict__ re, double* __restrict__ im, uint64_t N) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < N; i += (uint64_t)gridDim.x * blockDim.x) {
+    const df64 a = reinterpret_cast<const df64*>(re)[i], b = reinterpret_cast<const df64*>(im)[i];
+    re[i] = (double)a.hi + (double)a.lo;
+    im[i] = (double)b.hi + (double)b.lo;
+  }
+}
+cudaError_t launch_to_df64(void* re, void* im, uint64_t N, unsigned grid, cudaStream_t s) {
+  k_to_df64<<<grid, 256, 0, s>>>((double*)re, (double*)im, N);
+  return cudaGetLastError();
+}
+cudaError_t launch_from_df64(void* re, void* im, uint64_t N, unsigned grid, cudaStream_t s) {
+  k_from_df64<<<grid, 256, 0, s>>>((double*)re, (double*)im, N);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------- conj transpose

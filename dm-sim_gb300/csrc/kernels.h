@@ -5,20 +5,27 @@
 
 namespace dmg {
 
+// Arithmetic of a pass: the state's element type.
+enum Arith : int { AR_FP64 = 0, AR_FP32 = 1, AR_DF64 = 2 };
+
 struct LaunchArgs {
-  void* re;            // device real parts (double or float)
+  void* re;            // device real parts (double, float, or double-float pairs)
   void* im;            // device imaginary parts
   const void* desc;    // device PassDesc<K>
   int K, cls;
-  bool fp32;
+  bool fp32;           // complex64 state
+  int arith;           // Arith
   unsigned grid;       // blocks
   int tile_entries;    // G * 4^K
 };
 
 // Launch one pass on stream s.
 cudaError_t launch_pass(const LaunchArgs& a, cudaStream_t s);
-// Resident blocks per SM of the kernel instance for (K, cls, precision).
-int pass_blocks_per_sm(int K, int cls, bool fp32);
+// Resident blocks per SM of the kernel instance for (K, cls, arithmetic).
+int pass_blocks_per_sm(int K, int cls, int arith);
+// In place: FP64 entries <-> double-float pairs (the fused path's working format)
+cudaError_t launch_to_df64(void* re, void* im, uint64_t N, unsigned grid, cudaStream_t s);
+cudaError_t launch_from_df64(void* re, void* im, uint64_t N, unsigned grid, cudaStream_t s);
 // In place A'[x*2^n + y] = conj(A[y*2^n + x]) (the reference's adjoint stage)
 cudaError_t launch_conj_transpose(void* re, void* im, int n, bool fp32, unsigned grid, cudaStream_t s);
 // rho <- |0..0><0..0|

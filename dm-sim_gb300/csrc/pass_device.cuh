@@ -17,15 +17,102 @@
 
 namespace dmg {
 
+// ---------------------------------------------------------------- df64
+// Double-float: an unevaluated sum hi + lo of two floats (|lo| <= ulp(hi)/2),
+// a 48-bit significand held in the 8 bytes of a double.  GB300's FP64 pipe
+// runs at 1/58 of the FP32 rate (1.21 vs 70.6 TFLOP/s measured), so fused
+// passes compute in df64 on the FP32 pipe.  Every operation is an error-free
+// transformation written with the _rn intrinsics, which the compiler never
+// contracts or reorders (TwoSum: Knuth; FastTwoSum: Dekker; TwoProd with FMA).
+struct __align__(8) df64 {
+  float hi, lo;
+  df64() = default;
+  __device__ __forceinline__ df64(float h, float l) : hi(h), lo(l) {}
+  __device__ __forceinline__ df64(int v) : hi((float)v), lo(0.f) {}
+  __device__ __forceinline__ explicit df64(double x) {
+    hi = __double2float_rn(x);
+    lo = __double2float_rn(x - (double)hi);
+  }
+};
+struct __align__(16) df64x2 {
+  df64 x, y;
+};
+
+__device__ __forceinline__ df64 two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float v = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v));
+  return df64(s, e);
+}
+__device__ __forceinline__ df64 fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return df64(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
+__device__ __forceinline__ df64 operator+(df64 a, df64 b) {
+  const df64 s = two_sum(a.hi, b.hi);
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ df64 operator*(df64 a, df64 b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return fast_two_sum(p, e);
+}
+// a*b + c in double-float
+__device__ __forceinline__ df64 df_fma(df64 a, df64 b, df64 c) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float pe = __fmaf_rn(a.hi, b.hi, -p);
+  pe = __fmaf_rn(a.hi, b.lo, pe);
+  pe = __fmaf_rn(a.lo, b.hi, pe);
+  const df64 s = two_sum(p, c.hi);
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(pe, c.lo)));
+}
+
+// a*b + c in the pass's arithmetic
+__device__ __forceinline__ double madd(double a, double b, double c) { return ::fma(a, b, c); }
+__device__ __forceinline__ float madd(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ df64 madd(df64 a, df64 b, df64 c) { return df_fma(a, b, c); }
+
 template <typename T> struct Vec2;
 template <> struct Vec2<double> { using type = double2; };
 template <> struct Vec2<float> { using type = float2; };
+template <> struct Vec2<df64> { using type = df64x2; };
+
+// L2-coherent 16-byte state accesses (in the batched work-queue kernel another
+// SM may have written a run earlier in the same launch; L1 is not coherent).
+template <typename T>
+__device__ __forceinline__ typename Vec2<T>::type ld2(const T* p) {
+  return __ldcg(reinterpret_cast<const typename Vec2<T>::type*>(p));
+}
+template <>
+__device__ __forceinline__ df64x2 ld2<df64>(const df64* p) {
+  const float4 v = __ldcg(reinterpret_cast<const float4*>(p));
+  df64x2 r;
+  r.x = df64(v.x, v.y);
+  r.y = df64(v.z, v.w);
+  return r;
+}
+template <typename T>
+__device__ __forceinline__ void st2(T* p, const typename Vec2<T>::type& v) {
+  __stcg(reinterpret_cast<typename Vec2<T>::type*>(p), v);
+}
+template <>
+__device__ __forceinline__ void st2<df64>(df64* p, const df64x2& v) {
+  __stcg(reinterpret_cast<float4*>(p), make_float4(v.x.hi, v.x.lo, v.y.hi, v.y.lo));
+}
+
+// Coefficients from the FP64 descriptor tables.
+template <typename T> __device__ __forceinline__ T coef(double x) { return (T)x; }
+template <> __device__ __forceinline__ df64 coef<df64>(double x) { return df64(x); }
 
 // Sign flip on the integer pipe (GB300's FP64 pipe is ~1/58 of the FP32 rate).
 __device__ __forceinline__ double flip(double x) {
   return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
 }
 __device__ __forceinline__ float flip(float x) { return __int_as_float(__float_as_int(x) ^ (int)0x80000000); }
+__device__ __forceinline__ df64 flip(df64 x) { return df64(flip(x.hi), flip(x.lo)); }
 
 template <int K>
 __device__ __forceinline__ int pext_local(int loc, const int* lpos) {
@@ -94,23 +181,23 @@ __device__ void load_tables(const PassDesc<K>* __restrict__ dp, PassTables<T, K,
   for (int i = tid; i < D * D; i += blockDim.x) {
     tb.fk[i] = dp->op.fk[i];
     if (PassTables<T, K, CLS>::kMat) {
-      tb.ure[i] = (T)dp->op.ure[i];
-      tb.uim[i] = (T)dp->op.uim[i];
-      tb.vre[i] = (T)dp->op.vre[i];
-      tb.vim[i] = (T)dp->op.vim[i];
+      tb.ure[i] = coef<T>(dp->op.ure[i]);
+      tb.uim[i] = coef<T>(dp->op.uim[i]);
+      tb.vre[i] = coef<T>(dp->op.vre[i]);
+      tb.vim[i] = coef<T>(dp->op.vim[i]);
     }
     if (CLS == CLS_SPARSE) {
       tb.col[i] = dp->op.col[i];
       tb.colb[i] = dp->op.colb[i];
     }
     if (CLS == CLS_PHASE) {
-      tb.fre[i] = (T)dp->op.fre[i];
-      tb.fim[i] = (T)dp->op.fim[i];
+      tb.fre[i] = coef<T>(dp->op.fre[i]);
+      tb.fim[i] = coef<T>(dp->op.fim[i]);
     }
   }
   if (CLS == CLS_RLIN && tid < 16) {
-    tb.rl[tid] = (T)dp->op.rlin[tid];
-    tb.rl[16 + tid] = (T)dp->op.rlinb[tid];
+    tb.rl[tid] = coef<T>(dp->op.rlin[tid]);
+    tb.rl[16 + tid] = coef<T>(dp->op.rlinb[tid]);
   }
 }
 
@@ -146,8 +233,8 @@ __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeade
     const int run = e >> L;
     if (!((tb.ldmask[run >> 5] >> (run & 31)) & 1)) continue;
     const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
-    const T2 vr = *reinterpret_cast<const T2*>(re + ga);
-    const T2 vi = *reinterpret_cast<const T2*>(im + ga);
+    const T2 vr = ld2<T>(re + ga);
+    const T2 vi = ld2<T>(im + ga);
     *reinterpret_cast<T2*>(sre + e) = vr;
     *reinterpret_cast<T2*>(sim + e) = vi;
   }
@@ -179,10 +266,10 @@ __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeade
 #pragma unroll
           for (int c = 0; c < D; c++) {
             const T ur = tb.ure[a * D + c], ui = tb.uim[a * D + c];
-            ar = fma(ur, xr[c], ar);
-            ar = fma(-ui, xi[c], ar);
-            ai = fma(ur, xi[c], ai);
-            ai = fma(ui, xr[c], ai);
+            ar = madd(ur, xr[c], ar);
+            ar = madd(-ui, xi[c], ar);
+            ai = madd(ur, xi[c], ai);
+            ai = madd(ui, xr[c], ai);
           }
           sre[cb + tb.lk[a]] = ar;
           sim[cb + tb.lk[a]] = ai;
@@ -197,10 +284,10 @@ __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeade
             const int c = tb.col[a * D + j];
             const T ur = tb.ure[a * D + c], ui = tb.uim[a * D + c];
             const T vr = sre[cb + tb.lk[c]], vi = sim[cb + tb.lk[c]];
-            ar = fma(ur, vr, ar);
-            ar = fma(-ui, vi, ar);
-            ai = fma(ur, vi, ai);
-            ai = fma(ui, vr, ai);
+            ar = madd(ur, vr, ar);
+            ar = madd(-ui, vi, ar);
+            ai = madd(ur, vi, ai);
+            ai = madd(ui, vr, ai);
           }
           yr[a] = ar;
           yi[a] = ai;
@@ -239,10 +326,10 @@ __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeade
 #pragma unroll
           for (int c = 0; c < D; c++) {
             const T vr = tb.vre[b * D + c], vi = tb.vim[b * D + c];
-            ar = fma(vr, xr[c], ar);
-            ar = fma(-vi, xi[c], ar);
-            ai = fma(vr, xi[c], ai);
-            ai = fma(vi, xr[c], ai);
+            ar = madd(vr, xr[c], ar);
+            ar = madd(-vi, xi[c], ar);
+            ai = madd(vr, xi[c], ai);
+            ai = madd(vi, xr[c], ai);
           }
           sre[ca + tb.lb[b]] = ar;
           sim[ca + tb.lb[b]] = ai;
@@ -257,10 +344,10 @@ __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeade
             const int c = tb.colb[b * D + j];
             const T mr = tb.vre[b * D + c], mi = tb.vim[b * D + c];
             const T vr = sre[ca + tb.lb[c]], vi = sim[ca + tb.lb[c]];
-            ar = fma(mr, vr, ar);
-            ar = fma(-mi, vi, ar);
-            ai = fma(mr, vi, ai);
-            ai = fma(mi, vr, ai);
+            ar = madd(mr, vr, ar);
+            ar = madd(-mi, vi, ar);
+            ai = madd(mr, vi, ai);
+            ai = madd(mi, vr, ai);
           }
           yr[b] = ar;
           yi[b] = ai;
@@ -279,8 +366,8 @@ __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeade
       const int run = e >> L;
       if (!((tb.stmask[run >> 5] >> (run & 31)) & 1)) continue;
       const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
-      *reinterpret_cast<T2*>(re + ga) = *reinterpret_cast<const T2*>(sre + e);
-      *reinterpret_cast<T2*>(im + ga) = *reinterpret_cast<const T2*>(sim + e);
+      st2<T>(re + ga, *reinterpret_cast<const T2*>(sre + e));
+      st2<T>(im + ga, *reinterpret_cast<const T2*>(sim + e));
     }
   } else {
     // ---- monomial: out[a][b] = f[a][b] * in[src[a]][srcb[b]], fused into the store
@@ -304,8 +391,8 @@ __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeade
           const int fk = tb.fk[a * D + b];
           if (CLS == CLS_PHASE && fk == FK_GEN) {
             const T fr = tb.fre[a * D + b], fi = tb.fim[a * D + b];
-            outr[u] = fma(fr, vr, -fi * vi);
-            outi[u] = fma(fr, vi, fi * vr);
+            outr[u] = madd(fr, vr, -fi * vi);
+            outi[u] = madd(fr, vi, fi * vr);
           } else if (fk == FK_ONE) {
             outr[u] = vr;
             outi[u] = vi;
@@ -327,8 +414,8 @@ __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeade
       wr.y = outr[1];
       wi.x = outi[0];
       wi.y = outi[1];
-      *reinterpret_cast<T2*>(re + ga) = wr;
-      *reinterpret_cast<T2*>(im + ga) = wi;
+      st2<T>(re + ga, wr);
+      st2<T>(im + ga, wi);
     }
   }
   __syncthreads();

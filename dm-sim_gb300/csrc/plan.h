@@ -28,6 +28,7 @@ struct PassSpec {
 // Cost-model features of one pass (also recorded with its measured time).
 struct PassFeatures {
   int K, cls, nnz;
+  int arith;        // 0 FP64, 1 FP32, 2 double-float
   int max_lo_bit;   // highest target bit below L (-1 if none)
   int min_hi_bit;   // lowest target bit at or above L (2n if none)
   int n;

@@ -13,7 +13,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.normpath(os.path.join(_HERE, "..", "lib", "libdmsim_gb300.so"))
 
 OK, ERR_ARG, ERR_STATE, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_UNSUPPORTED = range(7)
-OPT_MODE, OPT_PRECISION, OPT_MAX_K, OPT_PLANNER, OPT_RECORD, OPT_SEED, OPT_GRAPH, OPT_VERBOSE = range(1, 9)
+OPT_MODE, OPT_PRECISION, OPT_MAX_K, OPT_PLANNER, OPT_RECORD, OPT_SEED, OPT_GRAPH, OPT_VERBOSE, OPT_FUSED_ARITH = range(1, 10)
+AR_FP64, AR_FP32, AR_DF64 = 0, 1, 2
 
 OP_NAMES = ["U3", "U2", "U1", "CX", "ID", "X", "Y", "Z", "H", "S",
             "SDG", "T", "TDG", "RX", "RY", "RZ", "CZ", "CY", "SWAP", "CH",
@@ -74,7 +75,7 @@ def lib():
         "dmsim_compare_states": [H, H, P(d)],
         "dmsim_alloc_host": [ctypes.c_size_t, P(ctypes.c_void_p)],
         "dmsim_free_host": [ctypes.c_void_p],
-        "dmsim_cost_collect": [u32, u32, u32, u64, P(d), P(d), u32, P(u32)],
+        "dmsim_cost_collect": [u32, u32, u32, u64, ctypes.c_int, P(d), P(d), u32, P(u32)],
         "dmsim_cost_train": [P(d), P(d), u32, u32, d, u64, P(d)],
         "dmsim_cost_predict": [P(d), u32, P(d)],
         "dmsim_cost_save": [ctypes.c_char_p],
@@ -83,6 +84,16 @@ def lib():
         "dmsim_mlp_grad": [P(ctypes.c_float), P(ctypes.c_float), P(ctypes.c_float), u32, P(ctypes.c_float),
                            P(ctypes.c_float)],
         "dmsim_plan_predicted_ms": [H, P(d)],
+        "dmsim_batch_create": [u32, P(u32), P(H)],
+        "dmsim_batch_destroy": [H],
+        "dmsim_batch_set_option": [H, ctypes.c_int, i64],
+        "dmsim_batch_append": [H, u32, ctypes.c_int, P(u32), d, d, d],
+        "dmsim_batch_upload": [H],
+        "dmsim_batch_run": [H],
+        "dmsim_batch_get_diag": [H, u32, P(d)],
+        "dmsim_batch_get_zz": [H, u32, P(d)],
+        "dmsim_batch_get_dm": [H, u32, P(d), P(d)],
+        "dmsim_batch_stats": [H, P(d)],
         "dmsim_plan_inspect": [u32, P(ctypes.c_int32), P(u32), P(d), P(d), u32, ctypes.c_int, ctypes.c_int,
                                ctypes.c_int, P(d), u32, P(u32)],
     }
@@ -92,6 +103,8 @@ def lib():
         f.restype = ctypes.c_int
     L.dmsim_last_error.argtypes = [H]
     L.dmsim_last_error.restype = ctypes.c_char_p
+    L.dmsim_batch_last_error.argtypes = [H]
+    L.dmsim_batch_last_error.restype = ctypes.c_char_p
     L.dmsim_status_string.argtypes = [ctypes.c_int]
     L.dmsim_status_string.restype = ctypes.c_char_p
     _lib = L
@@ -111,7 +124,7 @@ class Simulation:
     """
 
     def __init__(self, n_qubits, n_gpus=1, precision="fp64", mode="plain", max_k=4, planner="greedy",
-                 graph=True):
+                 graph=True, fused_arith="df64"):
         self._h = ctypes.c_void_p()
         self.n = int(n_qubits)
         st = lib().dmsim_create(self.n, int(n_gpus), ctypes.byref(self._h))
@@ -123,6 +136,7 @@ class Simulation:
             self.set_option(OPT_MAX_K, int(max_k))
             self.set_option(OPT_PLANNER, 1 if planner == "learned" else 0)
             self.set_option(OPT_GRAPH, 1 if graph else 0)
+            self.set_option(OPT_FUSED_ARITH, 1 if fused_arith == "df64" else 0)
         except Exception:
             self.close()
             raise
@@ -376,13 +390,15 @@ def _ok(st, what):
         raise DMSimError(st, f"{what}: {lib().dmsim_status_string(st).decode()}")
 
 
-def cost_collect(n, n_circuits=2, gates=60, seed=0, cap=200000):
+def cost_collect(n, n_circuits=2, gates=60, seed=0, arith=AR_DF64, cap=200000):
     """Per-pass (features, ms) samples the engine records on its own random
-    circuits under several fusion plans, timed with CUDA events on the GPU."""
+    circuits under several fusion plans, timed with CUDA events on the GPU,
+    in the given arithmetic (AR_FP64 or AR_DF64)."""
     feats = np.zeros((cap, COST_FEATURES))
     ms = np.zeros(cap)
     cnt = ctypes.c_uint32()
-    _ok(lib().dmsim_cost_collect(n, n_circuits, gates, seed, _dp(feats), _dp(ms), cap, ctypes.byref(cnt)), "cost_collect")
+    _ok(lib().dmsim_cost_collect(n, n_circuits, gates, seed, arith, _dp(feats), _dp(ms), cap, ctypes.byref(cnt)),
+        "cost_collect")
     k = min(cnt.value, cap)
     return feats[:k].copy(), ms[:k].copy()
 
@@ -426,3 +442,78 @@ def mlp_grad(params, X, T):
     loss = np.zeros(1, dtype=np.float32)
     _ok(lib().dmsim_mlp_grad(_fp(params), _fp(X), _fp(T), len(X), _fp(g), _fp(loss)), "mlp_grad")
     return g, float(loss[0])
+
+
+class Batch:
+    """Many independent circuits (1..16 qubits each, uneven counts allowed),
+    each from |0..0><0..0|, run together by one persistent work-queue kernel
+    from one captured CUDA graph.  Outputs per circuit: the diagonal and
+    <Z_i Z_{i+1}>."""
+
+    def __init__(self, n_qubits_list, mode="fused", max_k=4, planner="greedy"):
+        self.nq = [int(x) for x in n_qubits_list]
+        self._h = ctypes.c_void_p()
+        arr = (ctypes.c_uint32 * len(self.nq))(*self.nq)
+        st = lib().dmsim_batch_create(len(self.nq), arr, ctypes.byref(self._h))
+        if st != OK:
+            raise DMSimError(st, lib().dmsim_status_string(st).decode())
+        self._check(lib().dmsim_batch_set_option(self._h, OPT_MODE, 1 if mode == "fused" else 0))
+        self._check(lib().dmsim_batch_set_option(self._h, OPT_MAX_K, int(max_k)))
+        self._check(lib().dmsim_batch_set_option(self._h, OPT_PLANNER, 1 if planner == "learned" else 0))
+
+    def _check(self, st):
+        if st != OK:
+            raise DMSimError(st, lib().dmsim_batch_last_error(self._h).decode())
+
+    def close(self):
+        if self._h:
+            lib().dmsim_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def append(self, c, op, qubits, theta=0.0, phi=0.0, lam=0.0):
+        q = list(qubits) + [0] * (5 - len(qubits))
+        self._check(lib().dmsim_batch_append(self._h, c, int(op), (ctypes.c_uint32 * 5)(*q), theta, phi, lam))
+
+    def extend(self, c, circuit):
+        for g in circuit:
+            self.append(c, g[0], g[1], g[2], g[3], g[4])
+
+    def upload(self):
+        self._check(lib().dmsim_batch_upload(self._h))
+
+    def run(self):
+        self._check(lib().dmsim_batch_run(self._h))
+
+    def diag(self, c):
+        out = np.zeros(1 << self.nq[c])
+        self._check(lib().dmsim_batch_get_diag(self._h, c, _dp(out)))
+        return out
+
+    def zz(self, c):
+        out = np.zeros(max(self.nq[c] - 1, 1))
+        self._check(lib().dmsim_batch_get_zz(self._h, c, _dp(out)))
+        return out[:max(self.nq[c] - 1, 0)]
+
+    def dm(self, c):
+        N = 1 << (2 * self.nq[c])
+        re, im = np.zeros(N), np.zeros(N)
+        self._check(lib().dmsim_batch_get_dm(self._h, c, _dp(re), _dp(im)))
+        return re, im
+
+    def stats(self):
+        o = np.zeros(6)
+        self._check(lib().dmsim_batch_stats(self._h, _dp(o)))
+        return {"ms": o[0], "passes": int(o[1]), "basic": int(o[2]), "items": int(o[3]), "bytes": o[4],
+                "grid": int(o[5])}

@@ -40,7 +40,8 @@ enum dmsim_option {
   DMSIM_OPT_RECORD = 5,     /* 1 = time every pass of the next runs (no graph) [0] */
   DMSIM_OPT_SEED = 6,       /* seed of measure() without uniforms; -1 = time(0) like the reference [-1] */
   DMSIM_OPT_GRAPH = 7,      /* 1 = replay uploaded circuits from a captured CUDA graph [1] */
-  DMSIM_OPT_VERBOSE = 8     /* 1 = print the reference's per-run timing banner [0] */
+  DMSIM_OPT_VERBOSE = 8,    /* 1 = print the reference's per-run timing banner [0] */
+  DMSIM_OPT_FUSED_ARITH = 9 /* fused FP64 runs: 1 = double-float passes on the FP32 pipe [1], 0 = FP64 passes */
 };
 
 /* Gate ids: the order of enum OP, src/dmsim_nvgpu_omp.cuh:42-48 (ABI). */
@@ -144,14 +145,14 @@ int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qu
  * touched fractions, target-bit positions, size, precision).
  * dmsim_cost_collect: run the engine's own random circuits (29-entry mixed
  * table, n qubits, mt19937_64 from seed) under several fusion plans on the
- * current GPU, timing every pass with CUDA events; writes up to cap samples
- * and the total count.  dmsim_cost_train: fit the network on the GPU (Adam,
+ * current GPU in the given arithmetic (0 FP64, 2 double-float), timing every
+ * pass with CUDA events; writes up to cap samples and the total count.  dmsim_cost_train: fit the network on the GPU (Adam,
  * full batch, steps, lr, weights seeded by seed); loss[0..1] = first / last
  * mean squared error of standardised log time.  dmsim_cost_predict: GPU
  * inference, ms per sample.  save / load: the weights file. */
 #define DMSIM_COST_FEATURES 16
-int dmsim_cost_collect(uint32_t n, uint32_t n_circuits, uint32_t gates, uint64_t seed, double* feats, double* ms,
-                       uint32_t cap, uint32_t* count);
+int dmsim_cost_collect(uint32_t n, uint32_t n_circuits, uint32_t gates, uint64_t seed, int arith, double* feats,
+                       double* ms, uint32_t cap, uint32_t* count);
 int dmsim_cost_train(const double* feats, const double* ms, uint32_t count, uint32_t steps, double lr, uint64_t seed,
                      double loss[2]);
 int dmsim_cost_predict(const double* feats, uint32_t count, double* out_ms);
@@ -164,6 +165,27 @@ int dmsim_mlp_forward(const float* params, const float* X, uint32_t B, float* y)
 int dmsim_mlp_grad(const float* params, const float* X, const float* T, uint32_t B, float* grad, float* loss);
 /* Predicted run time of the uploaded plan (learned planner), ms */
 int dmsim_plan_predicted_ms(dmsim_handle h, double* ms);
+/* ---- batched sweep: many independent circuits in one persistent launch ----
+ * Circuits of 1..16 qubits (uneven counts allowed), each from |0..0><0..0|,
+ * planned like single circuits (DMSIM_OPT_MODE / MAX_K / PLANNER via
+ * dmsim_batch_set_option), run by one work-queue kernel replayed from a
+ * captured CUDA graph.  Outputs per circuit: the diagonal (2^n) and
+ * <Z_i Z_{i+1}> for i < n-1.  stats: {ms of the last run, passes, basic
+ * gates, work items, algorithmic bytes, grid}.  No reference counterpart: the
+ * reference runs circuits one Simulation at a time. */
+typedef struct dmsim_batch* dmsim_batch_handle;
+int dmsim_batch_create(uint32_t n_circuits, const uint32_t* n_qubits, dmsim_batch_handle* out);
+int dmsim_batch_destroy(dmsim_batch_handle b);
+int dmsim_batch_set_option(dmsim_batch_handle b, int key, int64_t value);
+int dmsim_batch_append(dmsim_batch_handle b, uint32_t circuit, int op, const uint32_t qb[5], double theta, double phi,
+                       double lambda);
+int dmsim_batch_upload(dmsim_batch_handle b);
+int dmsim_batch_run(dmsim_batch_handle b);
+int dmsim_batch_get_diag(dmsim_batch_handle b, uint32_t circuit, double* out);
+int dmsim_batch_get_zz(dmsim_batch_handle b, uint32_t circuit, double* out);
+int dmsim_batch_get_dm(dmsim_batch_handle b, uint32_t circuit, double* re, double* im);
+int dmsim_batch_stats(dmsim_batch_handle b, double out[6]);
+const char* dmsim_batch_last_error(dmsim_batch_handle b);
 /* Device pointers of rho (for in-HBM benchmarks and interop) */
 int dmsim_device_state(dmsim_handle h, void** re, void** im);
 const char* dmsim_last_error(dmsim_handle h);

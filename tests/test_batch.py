@@ -1,0 +1,62 @@
+"""The batched sweep: many circuits of uneven qubit counts in one persistent
+work-queue launch, each checked against the oracle; diagonal and <Z_i Z_{i+1}>
+outputs; the sweep workload's shape at a reduced size."""
+import numpy as np
+import pytest
+
+import dmsim_workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def zz_from_diag(diag, n):
+    idx = np.arange(1 << n)
+    return np.array([np.sum(diag * (1 - 2 * (((idx >> i) ^ (idx >> (i + 1))) & 1))) for i in range(n - 1)])
+
+
+@pytest.mark.parametrize("mode", ["plain", "fused"])
+def test_batch_matches_oracle(engine, oracle, mode):
+    rng = np.random.default_rng(5)
+    sweep = []
+    for i in range(12):
+        n = int(rng.integers(3, 9))
+        if i % 2:
+            sweep.append((n, W.hea(n, int(rng.integers(2, 5)), rng)))
+        else:
+            sweep.append((n, W.random_circuit(n, 30, ops=[o for o in range(38) if o != W.OP["SRN"]], seed=700 + i)))
+    with engine.Batch([n for n, _ in sweep], mode=mode) as b:
+        for c, (n, circ) in enumerate(sweep):
+            b.extend(c, circ)
+        b.upload()
+        for _ in range(2):  # the graph resets every state: two runs give the same result
+            b.run()
+            for c, (n, circ) in enumerate(sweep):
+                ref = oracle.dm_sim(n, circ)
+                re, im = b.dm(c)
+                scale = max(1.0, np.abs(ref[0]).max())
+                tol = (1e-12 if mode == "plain" else 1e-10) * scale
+                assert np.abs(re - ref[0]).max() <= tol and np.abs(im - ref[1]).max() <= tol, (c, n)
+                d = 1 << n
+                rd = ref[0].reshape(d, d).diagonal()
+                assert np.abs(b.diag(c) - rd).max() <= tol
+                if n > 1:
+                    assert np.abs(b.zz(c) - zz_from_diag(rd, n)).max() <= 10 * tol
+
+
+def test_hea_sweep_shape(engine, oracle):
+    """The parameter-sweep workload's shape (HEA, qubits uniform in {6..12}),
+    64 circuits: every output against the oracle's diagonal."""
+    sweep = W.hea_sweep(64, seed=9, nmin=6, nmax=10)
+    with engine.Batch([n for n, _ in sweep], mode="fused") as b:
+        for c, (n, circ) in enumerate(sweep):
+            b.extend(c, circ)
+        b.upload()
+        b.run()
+        st = b.stats()
+        assert st["ms"] > 0 and st["items"] > 0
+        for c in (0, 7, 31, 63):
+            n, circ = sweep[c]
+            sr, si = oracle.sv_sim(n, circ)
+            p = sr ** 2 + si ** 2
+            assert np.abs(b.diag(c) - p).max() <= 1e-10
+            assert np.abs(b.zz(c) - zz_from_diag(p, n)).max() <= 1e-9
