@@ -139,6 +139,115 @@ def run_reference_arm(args, n, circ):
     print(json.dumps(line))
 
 
+def timed_runs(sim, warmup, steps):
+    for _ in range(warmup):
+        sim.run()
+    ms = []
+    for _ in range(steps):
+        sim.run()
+        ms.append(sim.last_timings()["ms"])
+    return float(np.mean(ms))
+
+
+def extra_workload(args):
+    """Measurements beside the bench line (same device timing rules)."""
+    import dmsim_gb300 as E
+    out = {"workload": args.workload, "steps": args.steps, "warmup": args.warmup}
+    clocks = ClockSampler()
+    if args.workload == "sweep":
+        # 512 hardware-efficient-ansatz circuits, qubits uniform in {6..12},
+        # 4-10 layers; one persistent graph-captured launch vs sequential plain runs
+        sweep = W.hea_sweep(512, seed=4)
+        b = E.Batch([n for n, _ in sweep], mode="fused", max_k=args.max_k)
+        for c, (n, circ) in enumerate(sweep):
+            b.extend(c, circ)
+        b.upload()
+        out["autotune_best_ms"] = b.autotune()
+        for _ in range(args.warmup):
+            b.run()
+        clocks.start()
+        ms = []
+        for _ in range(args.steps):
+            b.run()
+            ms.append(b.stats()["ms"])
+        out["clocks"] = clocks.stop()
+        st = b.stats()
+        out["batched_s"] = float(np.mean(ms)) / 1e3
+        out["batched_circuits_per_s"] = 512 / out["batched_s"]
+        out["batch_stats"] = st
+        out["batched_GBps"] = st["bytes"] / (out["batched_s"]) / 1e9
+        seq = 0.0
+        worst = 0.0
+        for c, (n, circ) in enumerate(sweep):
+            with E.Simulation(n, mode="plain") as s:
+                s.extend(circ)
+                s.upload()
+                s.run()
+                s.run()  # second replay: no first-launch effects
+                seq += s.last_timings()["ms"]
+                if c % 37 == 0:
+                    s.reset_dm()
+                    s.run()
+                    worst = max(worst, float(np.abs(s.get_diag() - b.diag(c)).max()))
+        out["sequential_plain_s"] = seq / 1e3
+        out["sequential_plain_circuits_per_s"] = 512 / out["sequential_plain_s"]
+        out["speedup_batched_vs_sequential"] = out["sequential_plain_s"] / out["batched_s"]
+        out["diag_max_abs_err_vs_plain"] = worst
+        b.close()
+    elif args.workload == "qft16":
+        n = 16
+        circ = W.qft_then_layers(n, 1000, seed=3)
+        fused = E.Simulation(n, mode="fused", max_k=args.max_k, planner=args.planner)
+        fused.extend(circ)
+        fused.upload()
+        clocks.start()
+        out["fused_s"] = timed_runs(fused, args.warmup, args.steps) / 1e3
+        out["clocks"] = clocks.stop()
+        out["fused_passes"], out["basic_gates"] = fused.plan_stats()
+        out["fused_GBps"] = fused.last_timings()["bytes"] / out["fused_s"] / 1e9
+        fused.reset_dm()
+        fused.run()
+        if not args.no_plain:
+            plain = E.Simulation(n, mode="plain")
+            plain.extend(circ)
+            plain.upload()
+            plain.run()
+            out["plain_s"] = plain.last_timings()["ms"] / 1e3
+            out["plain_GBps"] = plain.last_timings()["bytes"] / out["plain_s"] / 1e9
+            out["speedup_fused_vs_plain"] = out["plain_s"] / out["fused_s"]
+            out["fused_vs_plain_error"] = fused.compare(plain)
+            plain.close()
+        fused.close()
+    elif args.workload == "c64_17":
+        n = 17
+        circ = W.u3_cx_ccx(n, 1000, seed=5)
+        s = E.Simulation(n, mode="fused", max_k=args.max_k, precision="c64", planner=args.planner)
+        s.extend(circ)
+        s.upload()
+        clocks.start()
+        out["c64_s"] = timed_runs(s, args.warmup, args.steps) / 1e3
+        out["clocks"] = clocks.stop()
+        out["passes"], out["basic_gates"] = s.plan_stats()
+        out["c64_GBps"] = s.last_timings()["bytes"] / out["c64_s"] / 1e9
+        d = s.get_diag()
+        out["trace_fp64_sum"] = float(d.sum())
+        s.close()
+        # the same circuit truncated to its first 16 qubits: complex64 against FP64
+        trunc = [g for g in circ if max(g[1]) < 16]
+        a = E.Simulation(16, mode="fused", max_k=args.max_k, precision="c64")
+        a.extend(trunc)
+        a.upload()
+        a.run()
+        bsim = E.Simulation(16, mode="fused", max_k=args.max_k)
+        bsim.extend(trunc)
+        bsim.upload()
+        bsim.run()
+        out["c64_vs_fp64_16q"] = a.compare(bsim)
+        a.close()
+        bsim.close()
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -153,7 +262,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--workload", default="table14",
+                    help="table14 (the bench line), or extra measurements: sweep, qft16, c64_17")
     args = ap.parse_args()
+    if args.workload != "table14":
+        return extra_workload(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

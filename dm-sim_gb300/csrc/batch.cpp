@@ -42,6 +42,10 @@ struct dmsim_batch {
   bool uploaded = false;
   uint64_t n_passes = 0, n_basic = 0;
   double bytes = 0, last_ms = 0;
+  std::vector<std::vector<PassSpec>> plans;
+  // tile shape: circuits of at most small_n qubits get log2(groups per tile)
+  // reduced by g_shift (smaller tiles, more blocks on a small state)
+  int small_n = 0, g_shift = 0;
   std::string err;
 };
 
@@ -88,29 +92,11 @@ void free_plan(dmsim_batch* b) {
   b->uploaded = false;
 }
 
-void upload(dmsim_batch* b) {
-  if (b->uploaded) throw BErr{DMSIM_ERR_STATE, "upload() called twice"};
+// Descriptors (per circuit, per pass, with the current tile shape),
+// layer-major ranges, and the captured graph.
+void build(dmsim_batch* b) {
   const int nc = (int)b->nq.size();
-  // plan every circuit
-  std::vector<std::vector<PassSpec>> plans(nc);
-  b->n_passes = b->n_basic = 0;
-  for (int c = 0; c < nc; c++) {
-    std::vector<Basic> basics;
-    for (const GateRec& g : b->circ[c]) decompose(g, basics);
-    bool rlin = false;
-    for (const Basic& x : basics) rlin |= x.kind == BK_RLIN;
-    if (rlin) throw BErr{DMSIM_ERR_UNSUPPORTED, "the batched sweep does not take SRN (run such circuits singly)"};
-    if (b->mode == 0) plans[c] = plan_plain(basics);
-    else if (b->planner == 1) {
-      CostModel& m = global_cost_model();
-      if (!m.ready) throw BErr{DMSIM_ERR_STATE, "the learned planner needs a trained or loaded cost model"};
-      std::string err;
-      plans[c] = plan_learned(basics, (int)b->nq[c], b->maxk, AR_FP64, m, nullptr, err);
-      if (!err.empty()) throw BErr{DMSIM_ERR_CUDA, err};
-    } else plans[c] = plan_greedy(basics, b->maxk);
-    b->n_passes += plans[c].size();
-    b->n_basic += basics.size();
-  }
+  const std::vector<std::vector<PassSpec>>& plans = b->plans;
   // descriptors (per circuit, per pass) and layer-major ranges
   size_t maxp = 0;
   for (auto& p : plans) maxp = std::max(maxp, p.size());
@@ -128,7 +114,8 @@ void upload(dmsim_batch* b) {
       blob.resize(off + ((desc_size(ps.K) + 255) & ~(size_t)255));
       uint64_t ntiles = 0;
       int tile = 0;
-      const uint64_t entries = build_desc(ps, (int)b->nq[c], blob.data() + off, nullptr, &ntiles, &tile);
+      const int g_cap = (int)b->nq[c] <= b->small_n ? std::max(0, 8 - ps.K - b->g_shift) : 8;
+      const uint64_t entries = build_desc(ps, (int)b->nq[c], blob.data() + off, nullptr, &ntiles, &tile, g_cap);
       bytes += 16.0 * (double)entries;
       BatchRange r;
       std::memset(&r, 0, sizeof r);
@@ -186,6 +173,33 @@ void upload(dmsim_batch* b) {
     b->gexec = nullptr;
     throw BErr{DMSIM_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e)};
   }
+}
+
+void upload(dmsim_batch* b) {
+  if (b->uploaded) throw BErr{DMSIM_ERR_STATE, "upload() called twice"};
+  const int nc = (int)b->nq.size();
+  // plan every circuit
+  std::vector<std::vector<PassSpec>> plans(nc);
+  b->n_passes = b->n_basic = 0;
+  for (int c = 0; c < nc; c++) {
+    std::vector<Basic> basics;
+    for (const GateRec& g : b->circ[c]) decompose(g, basics);
+    bool rlin = false;
+    for (const Basic& x : basics) rlin |= x.kind == BK_RLIN;
+    if (rlin) throw BErr{DMSIM_ERR_UNSUPPORTED, "the batched sweep does not take SRN (run such circuits singly)"};
+    if (b->mode == 0) plans[c] = plan_plain(basics);
+    else if (b->planner == 1) {
+      CostModel& m = global_cost_model();
+      if (!m.ready) throw BErr{DMSIM_ERR_STATE, "the learned planner needs a trained or loaded cost model"};
+      std::string err;
+      plans[c] = plan_learned(basics, (int)b->nq[c], b->maxk, AR_FP64, m, nullptr, err);
+      if (!err.empty()) throw BErr{DMSIM_ERR_CUDA, err};
+    } else plans[c] = plan_greedy(basics, b->maxk);
+    b->n_passes += plans[c].size();
+    b->n_basic += basics.size();
+  }
+  b->plans = std::move(plans);
+  build(b);
   b->uploaded = true;
 }
 
@@ -316,6 +330,45 @@ int dmsim_batch_run(dmsim_batch_handle b) {
   });
 }
 
+int dmsim_batch_autotune(dmsim_batch_handle b, double* best_ms) {
+  return guard(b, [&] {
+    if (!b->uploaded) throw BErr{DMSIM_ERR_STATE, "autotune() before upload()"};
+    struct Cfg {
+      int small_n, g_shift;
+    };
+    const Cfg cands[] = {{0, 0}, {8, 1}, {8, 2}, {10, 1}, {10, 2}, {12, 1}};
+    double best = 1e30;
+    Cfg pick = cands[0];
+    for (const Cfg& c : cands) {
+      free_plan(b);
+      b->small_n = c.small_n;
+      b->g_shift = c.g_shift;
+      build(b);
+      b->uploaded = true;
+      double t = 1e30;
+      for (int r = 0; r < 2; r++) {
+        B_CUDA(cudaEventRecord(b->ev0, b->stream));
+        B_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+        B_CUDA(cudaEventRecord(b->ev1, b->stream));
+        B_CUDA(cudaEventSynchronize(b->ev1));
+        float ms = 0;
+        B_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+        t = std::min(t, (double)ms);
+      }
+      if (t < best) {
+        best = t;
+        pick = c;
+      }
+    }
+    free_plan(b);
+    b->small_n = pick.small_n;
+    b->g_shift = pick.g_shift;
+    build(b);
+    b->uploaded = true;
+    if (best_ms) *best_ms = best;
+  });
+}
+
 int dmsim_batch_get_diag(dmsim_batch_handle b, uint32_t circuit, double* out) {
   return guard(b, [&] {
     if (!out || circuit >= b->nq.size()) throw BErr{DMSIM_ERR_ARG, "bad circuit index or null output"};
@@ -342,7 +395,7 @@ int dmsim_batch_get_dm(dmsim_batch_handle b, uint32_t circuit, double* re, doubl
   });
 }
 
-int dmsim_batch_stats(dmsim_batch_handle b, double out[6]) {
+int dmsim_batch_stats(dmsim_batch_handle b, double out[8]) {
   return guard(b, [&] {
     if (!out) throw BErr{DMSIM_ERR_ARG, "null output"};
     out[0] = b->last_ms;
@@ -351,6 +404,8 @@ int dmsim_batch_stats(dmsim_batch_handle b, double out[6]) {
     out[3] = (double)b->nitems;
     out[4] = b->bytes;
     out[5] = (double)b->grid;
+    out[6] = (double)b->small_n;
+    out[7] = (double)b->g_shift;
   });
 }
 

@@ -71,6 +71,7 @@ struct dmsim_sim {
 
   int mode = 0, maxk = 4, planner = 0, record = 0, graph_on = 1, verbose = 0;
   int fused_arith = 1;  // fused FP64 runs compute in double-float (1) or FP64 (0)
+  int renorm = 64;      // complex64: renormalise every renorm passes (0 = never)
   int arith = 0;        // arithmetic of the uploaded plan (kernels.h Arith)
   int64_t seed = -1;
 
@@ -135,6 +136,12 @@ void check_qubits(const dmsim_sim* s, const GateRec& g) {
 void enqueue_passes(dmsim_sim* s, bool timed) {
   for (size_t i = 0; i < s->passes.size(); i++) {
     PassInfo& p = s->passes[i];
+    if (p.renorm) {
+      if (timed) DM_CUDA(cudaEventRecord(p.ev0, s->stream));
+      DM_CUDA(launch_renormalise(s->d_re, s->d_im, (int)s->n, s->fp32, s->d_acc + 4, p.grid, s->stream));
+      if (timed) DM_CUDA(cudaEventRecord(p.ev1, s->stream));
+      continue;
+    }
     if (p.conv) {
       if (timed) DM_CUDA(cudaEventRecord(p.ev0, s->stream));
       if (p.conv == 1) DM_CUDA(launch_to_df64(s->d_re, s->d_im, s->N, p.grid, s->stream));
@@ -271,6 +278,15 @@ void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_b
     const uint64_t cap = (uint64_t)s->sms * (uint64_t)bps;
     pi.grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, cap));
     s->passes.push_back(pi);
+    // complex64: FP64 trace + Hermitian renormalisation every renorm passes and at the end
+    if (s->fp32 && s->renorm > 0 && ((i + 1) % (size_t)s->renorm == 0 || i + 1 == specs.size())) {
+      PassInfo rn;
+      std::memset(&rn, 0, sizeof rn);
+      rn.renorm = true;
+      rn.grid = (unsigned)s->sms * 8;
+      rn.bytes = 2.0 * 2.0 * (double)s->N * (double)esize(s);
+      s->passes.push_back(rn);
+    }
   }
   if (arith == AR_DF64) {
     PassInfo pi;
@@ -488,6 +504,11 @@ int dmsim_set_option(dmsim_handle s, int key, int64_t v) {
         if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set the fused arithmetic before upload()"};
         s->fused_arith = v != 0;
         break;
+      case DMSIM_OPT_RENORM:
+        if (v < 0) throw DmError{DMSIM_ERR_ARG, "renorm interval must be >= 0"};
+        if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set the renormalisation interval before upload()"};
+        s->renorm = (int)v;
+        break;
       default: throw DmError{DMSIM_ERR_ARG, "unknown option"};
     }
   });
@@ -506,6 +527,7 @@ int dmsim_get_option(dmsim_handle s, int key, int64_t* v) {
       case DMSIM_OPT_GRAPH: *v = s->graph_on; break;
       case DMSIM_OPT_VERBOSE: *v = s->verbose; break;
       case DMSIM_OPT_FUSED_ARITH: *v = s->fused_arith; break;
+      case DMSIM_OPT_RENORM: *v = s->renorm; break;
       default: throw DmError{DMSIM_ERR_ARG, "unknown option"};
     }
   });
@@ -732,11 +754,11 @@ int dmsim_pure_metrics(dmsim_handle s, const double* psi_re, const double* psi_i
 int dmsim_compare_states(dmsim_handle a, dmsim_handle b, double out[2]) {
   DM_TRY(a, {
     if (!b || !out) throw DmError{DMSIM_ERR_ARG, "null argument"};
-    if (a->N != b->N || a->fp32 != b->fp32) throw DmError{DMSIM_ERR_ARG, "states differ in size or precision"};
+    if (a->N != b->N) throw DmError{DMSIM_ERR_ARG, "states differ in size"};
     ensure_state(a);
     ensure_state(b);
     DM_CUDA(cudaStreamSynchronize(b->stream));
-    DM_CUDA(launch_compare(a->d_re, a->d_im, b->d_re, b->d_im, a->fp32, a->N, a->d_acc, a->sms, a->stream));
+    DM_CUDA(launch_compare(a->d_re, a->d_im, b->d_re, b->d_im, a->fp32, b->fp32, a->N, a->d_acc, a->sms, a->stream));
     double acc[2] = {0, 0};
     DM_CUDA(cudaMemcpyAsync(acc, a->d_acc, 2 * sizeof(double), cudaMemcpyDeviceToHost, a->stream));
     DM_CUDA(cudaStreamSynchronize(a->stream));

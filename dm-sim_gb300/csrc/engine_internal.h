@@ -11,6 +11,7 @@ struct PassInfo {
   int K, cls;
   bool transpose;       // the in-place conjugate transpose (reference-order plans)
   int conv;             // 1: FP64 -> double-float before a fused run, 2: back after it
+  bool renorm;          // complex64: FP64 trace + Hermitian renormalisation
   size_t desc_off;      // byte offset of the descriptor in the device blob
   int tile_entries;
   unsigned grid;

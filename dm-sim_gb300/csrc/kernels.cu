@@ -13,6 +13,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "kernels.h"
 #include "pass.h"
 #include "pass_device.cuh"
@@ -185,6 +187,79 @@ __global__ void __launch_bounds__(256) k_conj_transpose(T* __restrict__ re, T* _
 cudaError_t launch_conj_transpose(void* re, void* im, int n, bool fp32, unsigned grid, cudaStream_t s) {
   if (fp32) k_conj_transpose<float><<<grid, 256, 0, s>>>((float*)re, (float*)im, n);
   else k_conj_transpose<double><<<grid, 256, 0, s>>>((double*)re, (double*)im, n);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- renormalisation
+// complex64 mode: every R passes, trace(rho) is summed in FP64 and rho is made
+// Hermitian with unit trace, A <- (A + A^dagger) / (2 tr), in FP64 arithmetic
+// on the FP32 entries (tile pairs as in k_conj_transpose).
+template <typename T>
+__global__ void __launch_bounds__(256) k_trace(const T* __restrict__ re, int n, double* __restrict__ out) {
+  const uint64_t dim = 1ull << n;
+  double acc = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += (uint64_t)gridDim.x * blockDim.x)
+    acc += (double)re[i * dim + i];
+  __shared__ double sh[256];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(out, sh[0]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_hermitise(T* __restrict__ re, T* __restrict__ im, int n,
+                                                   const double* __restrict__ trace) {
+  constexpr int TS = 32;
+  __shared__ T a_re[TS][TS + 1], a_im[TS][TS + 1], b_re[TS][TS + 1], b_im[TS][TS + 1];
+  const uint64_t dim = 1ull << n;
+  const int ts = dim < TS ? (int)dim : TS;
+  const uint64_t nt = dim / ts;
+  const double inv = 1.0 / *trace;
+  const int tx = threadIdx.x & 31, ty0 = threadIdx.x >> 5;
+  for (uint64_t p = blockIdx.x; p < nt * nt; p += gridDim.x) {
+    const uint64_t I = p / nt, J = p % nt;
+    if (I > J) continue;
+    if (tx < ts)
+      for (int ty = ty0; ty < ts; ty += 8) {
+        const uint64_t ia = (I * ts + ty) * dim + J * ts + tx, ib = (J * ts + ty) * dim + I * ts + tx;
+        a_re[ty][tx] = re[ia];
+        a_im[ty][tx] = im[ia];
+        b_re[ty][tx] = re[ib];
+        b_im[ty][tx] = im[ib];
+      }
+    __syncthreads();
+    if (tx < ts)
+      for (int ty = ty0; ty < ts; ty += 8) {
+        const uint64_t ia = (I * ts + ty) * dim + J * ts + tx, ib = (J * ts + ty) * dim + I * ts + tx;
+        // new A[x][y] = (A[x][y] + conj(A[y][x])) / 2 / tr
+        const double ar = 0.5 * inv * ((double)a_re[ty][tx] + (double)b_re[tx][ty]);
+        const double ai = 0.5 * inv * ((double)a_im[ty][tx] - (double)b_im[tx][ty]);
+        const double br = 0.5 * inv * ((double)b_re[ty][tx] + (double)a_re[tx][ty]);
+        const double bi = 0.5 * inv * ((double)b_im[ty][tx] - (double)a_im[tx][ty]);
+        re[ia] = (T)ar;
+        im[ia] = (T)ai;
+        re[ib] = (T)br;
+        im[ib] = (T)bi;
+      }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_renormalise(void* re, void* im, int n, bool fp32, double* d_trace, unsigned grid, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(d_trace, 0, sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  const unsigned tg = (unsigned)std::min<uint64_t>((1ull << n) / 256 + 1, 1024);
+  if (fp32) {
+    k_trace<float><<<tg, 256, 0, s>>>((const float*)re, n, d_trace);
+    k_hermitise<float><<<grid, 256, 0, s>>>((float*)re, (float*)im, n, d_trace);
+  } else {
+    k_trace<double><<<tg, 256, 0, s>>>((const double*)re, n, d_trace);
+    k_hermitise<double><<<grid, 256, 0, s>>>((double*)re, (double*)im, n, d_trace);
+  }
   return cudaGetLastError();
 }
 

@@ -28,6 +28,8 @@ cudaError_t launch_to_df64(void* re, void* im, uint64_t N, unsigned grid, cudaSt
 cudaError_t launch_from_df64(void* re, void* im, uint64_t N, unsigned grid, cudaStream_t s);
 // In place A'[x*2^n + y] = conj(A[y*2^n + x]) (the reference's adjoint stage)
 cudaError_t launch_conj_transpose(void* re, void* im, int n, bool fp32, unsigned grid, cudaStream_t s);
+// rho <- (rho + rho^dagger) / (2 trace), trace summed in FP64 into d_trace
+cudaError_t launch_renormalise(void* re, void* im, int n, bool fp32, double* d_trace, unsigned grid, cudaStream_t s);
 // rho <- |0..0><0..0|
 cudaError_t launch_set_zero_state(void* re, void* im, uint64_t N, bool fp32, cudaStream_t s);
 // d_out[i] = Re rho[i][i] (FP64 whatever the state precision)

@@ -72,9 +72,9 @@ __global__ void __launch_bounds__(256) k_pure_metrics(const T* __restrict__ re, 
   }
 }
 
-template <typename T>
+template <typename T, typename U>
 __global__ void __launch_bounds__(256) k_compare(const T* __restrict__ ar, const T* __restrict__ ai,
-                                                 const T* __restrict__ br, const T* __restrict__ bi, uint64_t N,
+                                                 const U* __restrict__ br, const U* __restrict__ bi, uint64_t N,
                                                  double* acc) {
   double mx = 0, fro = 0;
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < N; v += (uint64_t)gridDim.x * blockDim.x) {
@@ -100,15 +100,19 @@ __global__ void __launch_bounds__(256) k_compare(const T* __restrict__ ar, const
   }
 }
 
-cudaError_t launch_compare(const void* ar, const void* ai, const void* br, const void* bi, bool fp32, uint64_t N,
-                           double* d_acc, int sms, cudaStream_t s) {
+cudaError_t launch_compare(const void* ar, const void* ai, const void* br, const void* bi, bool a_fp32, bool b_fp32,
+                           uint64_t N, double* d_acc, int sms, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(d_acc, 0, 2 * sizeof(double), s);
   if (e != cudaSuccess) return e;
   const unsigned grid = (unsigned)(sms * 4);
-  if (fp32)
-    k_compare<float><<<grid, 256, 0, s>>>((const float*)ar, (const float*)ai, (const float*)br, (const float*)bi, N, d_acc);
+  if (a_fp32 && b_fp32)
+    k_compare<float, float><<<grid, 256, 0, s>>>((const float*)ar, (const float*)ai, (const float*)br, (const float*)bi, N, d_acc);
+  else if (a_fp32)
+    k_compare<float, double><<<grid, 256, 0, s>>>((const float*)ar, (const float*)ai, (const double*)br, (const double*)bi, N, d_acc);
+  else if (b_fp32)
+    k_compare<double, float><<<grid, 256, 0, s>>>((const double*)ar, (const double*)ai, (const float*)br, (const float*)bi, N, d_acc);
   else
-    k_compare<double><<<grid, 256, 0, s>>>((const double*)ar, (const double*)ai, (const double*)br, (const double*)bi, N, d_acc);
+    k_compare<double, double><<<grid, 256, 0, s>>>((const double*)ar, (const double*)ai, (const double*)br, (const double*)bi, N, d_acc);
   return cudaGetLastError();
 }
 

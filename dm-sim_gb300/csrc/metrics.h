@@ -8,8 +8,8 @@ namespace dmg {
 cudaError_t launch_pure_metrics(const void* re, const void* im, bool fp32, const double* psi_re, const double* psi_im,
                                 int n, double* d_acc, int sms, cudaStream_t s);
 // d_acc[0] = max |A - B|^2, d_acc[1] = ||A - B||_F^2 over two states of N entries.
-cudaError_t launch_compare(const void* ar, const void* ai, const void* br, const void* bi, bool fp32, uint64_t N,
-                           double* d_acc, int sms, cudaStream_t s);
+cudaError_t launch_compare(const void* ar, const void* ai, const void* br, const void* bi, bool a_fp32, bool b_fp32,
+                           uint64_t N, double* d_acc, int sms, cudaStream_t s);
 // The no-allocation variant of the pure-state metrics: psi is staged in a
 // file-scope device array instead of a cudaMalloc'd buffer.  States of at most
 // kNoAllocMaxQubits qubits (2^16 amplitudes); calls share the array.

@@ -322,7 +322,8 @@ size_t desc_size(int K) {
 namespace {
 
 template <int K>
-uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, uint64_t* ntiles_out, int* tile_out) {
+uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, uint64_t* ntiles_out, int* tile_out,
+                 int g_cap) {
   constexpr int D = 1 << K;
   std::memset(d, 0, sizeof(*d));
   PassHeader& h = d->h;
@@ -340,7 +341,9 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
   std::vector<int> F;
   for (int b = 0; b < nb; b++)
     if (!std::binary_search(P.begin(), P.end(), b)) F.push_back(b);
-  int g = 8 - K;
+  // at least one free bit in the low run keeps runs >= 2 entries long (the
+  // kernels move entries in 16-byte pairs)
+  int g = std::min(8 - K, std::max(g_cap, 1));
   if (g > (int)F.size()) g = (int)F.size();
   // L: the position of the (g+1)-th free bit, so that exactly g free bits
   // and every target bit below it lie in the contiguous low run.
@@ -490,12 +493,13 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
 
 }  // namespace
 
-uint64_t build_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries) {
+uint64_t build_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries,
+                    int g_cap) {
   switch (p.K) {
-    case 1: return build_k<1>(p, n, static_cast<PassDesc<1>*>(out), f, ntiles, tile_entries);
-    case 2: return build_k<2>(p, n, static_cast<PassDesc<2>*>(out), f, ntiles, tile_entries);
-    case 3: return build_k<3>(p, n, static_cast<PassDesc<3>*>(out), f, ntiles, tile_entries);
-    default: return build_k<4>(p, n, static_cast<PassDesc<4>*>(out), f, ntiles, tile_entries);
+    case 1: return build_k<1>(p, n, static_cast<PassDesc<1>*>(out), f, ntiles, tile_entries, g_cap);
+    case 2: return build_k<2>(p, n, static_cast<PassDesc<2>*>(out), f, ntiles, tile_entries, g_cap);
+    case 3: return build_k<3>(p, n, static_cast<PassDesc<3>*>(out), f, ntiles, tile_entries, g_cap);
+    default: return build_k<4>(p, n, static_cast<PassDesc<4>*>(out), f, ntiles, tile_entries, g_cap);
   }
 }
 

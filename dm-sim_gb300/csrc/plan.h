@@ -58,6 +58,8 @@ size_t desc_size(int K);
 // Write the descriptor of pass p for an n-qubit state into out (desc_size bytes).
 // Returns the algorithmic bytes per entry-size unit moved by the pass
 // (entries read + entries written); features are filled when f != nullptr.
-uint64_t build_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries);
+// g_cap caps log2 of the groups per tile (the tile shape; 8 = the largest).
+uint64_t build_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries,
+                    int g_cap = 8);
 
 }  // namespace dmg

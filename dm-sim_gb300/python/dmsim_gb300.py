@@ -13,7 +13,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.normpath(os.path.join(_HERE, "..", "lib", "libdmsim_gb300.so"))
 
 OK, ERR_ARG, ERR_STATE, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_UNSUPPORTED = range(7)
-OPT_MODE, OPT_PRECISION, OPT_MAX_K, OPT_PLANNER, OPT_RECORD, OPT_SEED, OPT_GRAPH, OPT_VERBOSE, OPT_FUSED_ARITH = range(1, 10)
+(OPT_MODE, OPT_PRECISION, OPT_MAX_K, OPT_PLANNER, OPT_RECORD, OPT_SEED, OPT_GRAPH, OPT_VERBOSE, OPT_FUSED_ARITH,
+ OPT_RENORM) = range(1, 11)
 AR_FP64, AR_FP32, AR_DF64 = 0, 1, 2
 
 OP_NAMES = ["U3", "U2", "U1", "CX", "ID", "X", "Y", "Z", "H", "S",
@@ -94,6 +95,7 @@ def lib():
         "dmsim_batch_get_zz": [H, u32, P(d)],
         "dmsim_batch_get_dm": [H, u32, P(d), P(d)],
         "dmsim_batch_stats": [H, P(d)],
+        "dmsim_batch_autotune": [H, P(d)],
         "dmsim_plan_inspect": [u32, P(ctypes.c_int32), P(u32), P(d), P(d), u32, ctypes.c_int, ctypes.c_int,
                                ctypes.c_int, P(d), u32, P(u32)],
     }
@@ -124,7 +126,7 @@ class Simulation:
     """
 
     def __init__(self, n_qubits, n_gpus=1, precision="fp64", mode="plain", max_k=4, planner="greedy",
-                 graph=True, fused_arith="df64"):
+                 graph=True, fused_arith="df64", renorm=64):
         self._h = ctypes.c_void_p()
         self.n = int(n_qubits)
         st = lib().dmsim_create(self.n, int(n_gpus), ctypes.byref(self._h))
@@ -137,6 +139,7 @@ class Simulation:
             self.set_option(OPT_PLANNER, 1 if planner == "learned" else 0)
             self.set_option(OPT_GRAPH, 1 if graph else 0)
             self.set_option(OPT_FUSED_ARITH, 1 if fused_arith == "df64" else 0)
+            self.set_option(OPT_RENORM, int(renorm))
         except Exception:
             self.close()
             raise
@@ -513,7 +516,13 @@ class Batch:
         return re, im
 
     def stats(self):
-        o = np.zeros(6)
+        o = np.zeros(8)
         self._check(lib().dmsim_batch_stats(self._h, _dp(o)))
         return {"ms": o[0], "passes": int(o[1]), "basic": int(o[2]), "items": int(o[3]), "bytes": o[4],
-                "grid": int(o[5])}
+                "grid": int(o[5]), "small_n": int(o[6]), "g_shift": int(o[7])}
+
+    def autotune(self):
+        """Pick the tile shape (groups per tile of the small circuits) by timing."""
+        v = ctypes.c_double()
+        self._check(lib().dmsim_batch_autotune(self._h, ctypes.byref(v)))
+        return v.value

@@ -41,7 +41,8 @@ enum dmsim_option {
   DMSIM_OPT_SEED = 6,       /* seed of measure() without uniforms; -1 = time(0) like the reference [-1] */
   DMSIM_OPT_GRAPH = 7,      /* 1 = replay uploaded circuits from a captured CUDA graph [1] */
   DMSIM_OPT_VERBOSE = 8,    /* 1 = print the reference's per-run timing banner [0] */
-  DMSIM_OPT_FUSED_ARITH = 9 /* fused FP64 runs: 1 = double-float passes on the FP32 pipe [1], 0 = FP64 passes */
+  DMSIM_OPT_FUSED_ARITH = 9, /* fused FP64 runs: 1 = double-float passes on the FP32 pipe [1], 0 = FP64 passes */
+  DMSIM_OPT_RENORM = 10      /* complex64: FP64 trace + Hermitian renormalisation every R passes and at the end [64]; 0 = off */
 };
 
 /* Gate ids: the order of enum OP, src/dmsim_nvgpu_omp.cuh:42-48 (ABI). */
@@ -121,8 +122,9 @@ int dmsim_pure_metrics(dmsim_handle h, const double* psi_re, const double* psi_i
  * two handles on the same device -- race; serialise them.  Same outputs as
  * dmsim_pure_metrics; rho must already be allocated (DMSIM_ERR_STATE if not). */
 int dmsim_pure_metrics_noalloc(dmsim_handle h, const double* psi_re, const double* psi_im, double out[4]);
-/* Compare two states of the same size and precision on the device:
- * out[0] = max |A - B| over entries, out[1] = ||A - B||_F. */
+/* Compare two states of the same size on the device (either precision, e.g.
+ * a complex64 state against an FP64 one): out[0] = max |A - B| over entries,
+ * out[1] = ||A - B||_F. */
 int dmsim_compare_states(dmsim_handle a, dmsim_handle b, double out[2]);
 /* Page-locked host buffers for fast dmsim_get_dm / dmsim_set_dm copies. */
 int dmsim_alloc_host(size_t bytes, void** out);
@@ -171,7 +173,7 @@ int dmsim_plan_predicted_ms(dmsim_handle h, double* ms);
  * dmsim_batch_set_option), run by one work-queue kernel replayed from a
  * captured CUDA graph.  Outputs per circuit: the diagonal (2^n) and
  * <Z_i Z_{i+1}> for i < n-1.  stats: {ms of the last run, passes, basic
- * gates, work items, algorithmic bytes, grid}.  No reference counterpart: the
+ * gates, work items, algorithmic bytes, grid, tile-shape small_n, g_shift}.  No reference counterpart: the
  * reference runs circuits one Simulation at a time. */
 typedef struct dmsim_batch* dmsim_batch_handle;
 int dmsim_batch_create(uint32_t n_circuits, const uint32_t* n_qubits, dmsim_batch_handle* out);
@@ -184,7 +186,10 @@ int dmsim_batch_run(dmsim_batch_handle b);
 int dmsim_batch_get_diag(dmsim_batch_handle b, uint32_t circuit, double* out);
 int dmsim_batch_get_zz(dmsim_batch_handle b, uint32_t circuit, double* out);
 int dmsim_batch_get_dm(dmsim_batch_handle b, uint32_t circuit, double* re, double* im);
-int dmsim_batch_stats(dmsim_batch_handle b, double out[6]);
+/* The tile-shape autotuner: times the uploaded batch under a few tile shapes
+ * (fewer groups per tile for the small circuits) and keeps the fastest. */
+int dmsim_batch_autotune(dmsim_batch_handle b, double* best_ms);
+int dmsim_batch_stats(dmsim_batch_handle b, double out[8]);
 const char* dmsim_batch_last_error(dmsim_batch_handle b);
 /* Device pointers of rho (for in-HBM benchmarks and interop) */
 int dmsim_device_state(dmsim_handle h, void** re, void** im);

@@ -1,0 +1,63 @@
+"""Full-size parity, where the CPU density-matrix oracle cannot run: the device
+state against the statevector oracle (rho = psi psi^+; the workloads are
+noise-free unitary circuits from a pure state), through the device-side
+fidelity / trace / max-element comparison."""
+import math
+
+import numpy as np
+import pytest
+
+import dmsim_workloads as W
+
+pytestmark = [pytest.mark.gpu, pytest.mark.slow]
+
+
+def test_table_mix_14q_fused_full_circuit(engine, oracle):
+    """The whole 14-qubit mixed-table workload (2000 gates, 23 650 basic gates),
+    fused double-float passes: <= 1e-10 max element error, |1 - F| <= 1e-10."""
+    n = 14
+    circ = W.table_mix(n, 2000, seed=2)
+    sr, si = oracle.sv_sim(n, circ)
+    psi = sr + 1j * si
+    with engine.Simulation(n, mode="fused") as s:
+        s.extend(circ)
+        s.upload()
+        s.run()
+        m = s.pure_metrics(psi)
+    assert m["max_abs_err"] <= 1e-10, m
+    assert abs(1 - m["fidelity"]) <= 1e-10 and abs(1 - m["trace"]) <= 1e-10, m
+
+
+def test_u3_cx_ccx_17q_complex64(engine, oracle):
+    """17 qubits in complex64 (4^17 entries, 137 GB): the trace distance to the
+    FP64 statevector oracle, bounded by sqrt(1 - F) for a pure reference, is
+    within 1e-5; the FP64 renormalisation keeps the trace at 1."""
+    n = 17
+    circ = W.u3_cx_ccx(n, 1000, seed=5)
+    sr, si = oracle.sv_sim(n, circ)
+    psi = sr + 1j * si
+    with engine.Simulation(n, mode="fused", precision="c64") as s:
+        s.extend(circ)
+        s.upload()
+        s.run()
+        m = s.pure_metrics(psi)
+    assert math.sqrt(max(0.0, 1 - m["fidelity"])) <= 1e-5, m
+    assert abs(1 - m["trace"]) <= 1e-5, m
+
+
+def test_complex64_renormalisation(engine, oracle):
+    """After a complex64 run rho is Hermitian and has unit trace to FP32
+    precision; without renormalisation the FP32 drift shows."""
+    n = 8
+    circ = W.table_mix(n, 600, seed=13)
+    res = {}
+    for renorm in (64, 0):
+        with engine.Simulation(n, mode="plain", precision="c64", renorm=renorm) as s:
+            s.extend(circ)
+            s.upload()
+            s.run()
+            re, im = s.get_dm()
+        d = 1 << n
+        A = re.reshape(d, d) + 1j * im.reshape(d, d)
+        res[renorm] = (abs(np.trace(A).real - 1), np.abs(A - A.conj().T).max())
+    assert res[64][0] <= 1e-6 and res[64][1] <= 1e-7, res
