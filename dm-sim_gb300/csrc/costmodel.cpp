@@ -17,7 +17,9 @@ void pass_features(const PassFeatures& f, float* x) {
   const double nb = 2.0 * f.n;
   for (int i = 0; i < kMlpIn; i++) x[i] = 0.f;
   x[0] = f.K / 4.0f;
-  if (f.cls >= 0 && f.cls < CLS_COUNT) x[1 + f.cls] = 1.f;  // x[1..6] class one-hot
+  // x[1..6] class one-hot (a channel pass counts as dense)
+  const int cls = f.cls == CLS_SUPER ? CLS_DENSE : f.cls;
+  if (cls >= 0 && cls <= CLS_RLIN) x[1 + cls] = 1.f;
   const int D = 1 << f.K;
   x[7] = (float)f.nnz / (float)(D * D);           // density of U
   x[8] = (float)f.nnz / (float)D / 16.f;          // nonzeros per row

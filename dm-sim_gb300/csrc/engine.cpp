@@ -62,6 +62,7 @@ struct dmsim_sim {
   double* d_acc = nullptr;
 
   std::vector<GateRec> circuit;
+  std::vector<Channel> channels;  // superoperators of the circuit's noise channels
   bool uploaded = false;
   std::vector<PassInfo> passes;
   void* d_desc = nullptr;
@@ -122,7 +123,7 @@ void ensure_state(dmsim_sim* s) {
 }
 
 void check_qubits(const dmsim_sim* s, const GateRec& g) {
-  const int ar = gate_arity(g.op);
+  const int ar = g.op == OP_CHANNEL ? g.nq : gate_arity(g.op);
   if (ar == 0) throw DmError{DMSIM_ERR_ARG, "unknown gate id " + std::to_string(g.op)};
   // the reference asserts every qubit slot < n_qubits (:334-338)
   for (int i = 0; i < 5; i++)
@@ -224,9 +225,14 @@ void upload(dmsim_sim* s) {
   if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "upload() called twice without clear_circuit() (:347-350)"};
   ensure_state(s);
   std::vector<Basic> basics;
-  for (const GateRec& g : s->circuit) decompose(g, basics);
-  bool rlin = false;
-  for (const Basic& b : basics) rlin |= b.kind == BK_RLIN;
+  for (const GateRec& g : s->circuit) decompose(g, basics, &s->channels);
+  bool rlin = false, chan = false;
+  for (const Basic& b : basics) {
+    rlin |= b.kind == BK_RLIN;
+    chan |= b.kind == BK_SUPER;
+  }
+  if (rlin && chan)
+    throw DmError{DMSIM_ERR_UNSUPPORTED, "a circuit with SRN runs in the reference's order, which has no noise channels"};
   upload_specs(s, make_plan(s, basics), (uint32_t)basics.size(), run_arith(s, rlin));
 }
 
@@ -376,6 +382,7 @@ void clear_circuit(dmsim_sim* s) {
   }
   free_plan(s);
   s->circuit.clear();
+  s->channels.clear();
 }
 
 void reset_dm(dmsim_sim* s) {
@@ -576,6 +583,114 @@ int dmsim_append_c2(dmsim_handle s, uint32_t q1, uint32_t q2, const double m[32]
   });
 }
 
+namespace {
+// Kraus operators -> the superoperator S = sum_i K_i (x) conj(K_i) in the pass
+// sub-index order (bit i <-> qubit q[i]); the caller's 2-qubit matrices use the
+// C2 basis order (index 2*bit(q1) + bit(q2)), so the two bits are swapped here.
+void append_kraus(dmsim_sim* s, uint32_t nq, const uint32_t q[2], uint32_t nk, const cplx* kraus) {
+  if (nq < 1 || nq > 2) throw DmError{DMSIM_ERR_ARG, "channels act on 1 or 2 qubits"};
+  if (nk < 1 || nk > 16) throw DmError{DMSIM_ERR_ARG, "1 to 16 Kraus operators"};
+  GateRec g;
+  std::memset(&g, 0, sizeof g);
+  g.op = OP_CHANNEL;
+  g.nq = (int)nq;
+  if (nq == 1) g.qb[0] = q[0];
+  else {
+    g.qb[0] = q[1];  // pass sub-index bit 0 <-> the caller's second qubit
+    g.qb[1] = q[0];
+  }
+  check_qubits(s, g);
+  const int D = 1 << nq, DD = D * D;
+  auto sub = [&](int idx) {  // caller's index -> pass sub-index
+    if (nq == 1) return idx;
+    return ((idx >> 1) & 1) | ((idx & 1) << 1);
+  };
+  Channel ch;
+  std::memset(&ch, 0, sizeof ch);
+  ch.K = (int)nq;
+  for (uint32_t i = 0; i < nk; i++) {
+    const cplx* Km = kraus + (size_t)i * DD;
+    for (int a = 0; a < D; a++)
+      for (int c = 0; c < D; c++)
+        for (int b = 0; b < D; b++)
+          for (int e = 0; e < D; e++) {
+            const int A = sub(a), C = sub(c), B = sub(b), E = sub(e);
+            ch.S[(A * D + B) * DD + (C * D + E)] += Km[a * D + c] * std::conj(Km[b * D + e]);
+          }
+  }
+  g.chan = (int32_t)s->channels.size();
+  s->channels.push_back(ch);
+  s->circuit.push_back(g);
+}
+}  // namespace
+
+int dmsim_append_channel(dmsim_handle s, uint32_t nq, const uint32_t q[2], uint32_t n_kraus, const double* kraus) {
+  DM_TRY(s, {
+    if (!q || !kraus) throw DmError{DMSIM_ERR_ARG, "null argument"};
+    const int D = 1 << nq;
+    std::vector<cplx> K((size_t)n_kraus * D * D);
+    for (size_t i = 0; i < K.size(); i++) K[i] = cplx(kraus[2 * i], kraus[2 * i + 1]);
+    append_kraus(s, nq, q, n_kraus, K.data());
+  });
+}
+
+int dmsim_append_noise(dmsim_handle s, int kind, const uint32_t q[2], double p) {
+  DM_TRY(s, {
+    if (!q) throw DmError{DMSIM_ERR_ARG, "null qubits"};
+    if (!(p >= 0.0 && p <= 1.0)) throw DmError{DMSIM_ERR_ARG, "noise strength must be in [0, 1]"};
+    const cplx I(0, 1);
+    const cplx id[4] = {1, 0, 0, 1}, X[4] = {0, 1, 1, 0}, Y[4] = {0, -I, I, 0}, Z[4] = {1, 0, 0, -1};
+    std::vector<cplx> K;
+    uint32_t nq = 1, nk = 0;
+    auto add = [&](const cplx* m, double w) {
+      for (int i = 0; i < 4; i++) K.push_back(std::sqrt(w) * m[i]);
+      nk++;
+    };
+    switch (kind) {
+      case DMSIM_NOISE_DEPOLARIZING:  // rho -> (1-p) rho + p I/2
+        add(id, 1 - 3 * p / 4);
+        add(X, p / 4);
+        add(Y, p / 4);
+        add(Z, p / 4);
+        break;
+      case DMSIM_NOISE_AMPLITUDE_DAMPING: {
+        const cplx k0[4] = {1, 0, 0, std::sqrt(1 - p)}, k1[4] = {0, std::sqrt(p), 0, 0};
+        add(k0, 1);
+        add(k1, 1);
+        break;
+      }
+      case DMSIM_NOISE_PHASE_DAMPING: {
+        const cplx k0[4] = {1, 0, 0, std::sqrt(1 - p)}, k1[4] = {0, 0, 0, std::sqrt(p)};
+        add(k0, 1);
+        add(k1, 1);
+        break;
+      }
+      case DMSIM_NOISE_BIT_FLIP:
+        add(id, 1 - p);
+        add(X, p);
+        break;
+      case DMSIM_NOISE_PHASE_FLIP:
+        add(id, 1 - p);
+        add(Z, p);
+        break;
+      case DMSIM_NOISE_DEPOLARIZING2: {  // rho -> (1-p) rho + p I/4 on two qubits
+        nq = 2;
+        const cplx* P[4] = {id, X, Y, Z};
+        for (int i = 0; i < 4; i++)
+          for (int j = 0; j < 4; j++) {
+            const double w = (i == 0 && j == 0) ? 1 - 15 * p / 16 : p / 16;
+            for (int a = 0; a < 4; a++)
+              for (int c = 0; c < 4; c++) K.push_back(std::sqrt(w) * P[i][(a >> 1) * 2 + (c >> 1)] * P[j][(a & 1) * 2 + (c & 1)]);
+            nk++;
+          }
+        break;
+      }
+      default: throw DmError{DMSIM_ERR_ARG, "unknown noise kind"};
+    }
+    append_kraus(s, nq, q, nk, K.data());
+  });
+}
+
 int dmsim_upload(dmsim_handle s) { DM_TRY(s, upload(s)); }
 int dmsim_run(dmsim_handle s) { DM_TRY(s, run(s)); }
 int dmsim_clear_circuit(dmsim_handle s) { DM_TRY(s, clear_circuit(s)); }
@@ -667,7 +782,7 @@ int dmsim_dump(dmsim_handle s, char* buf, size_t len, size_t* needed) {
     // Gate::dump (:170-176): NAME(qb0,qb1,qb2,qb3,qb4,theta,phi,lambda);
     std::stringstream ss;
     for (const GateRec& g : s->circuit) {
-      const char* name = g.op == OP_C1 ? "C1" : g.op == OP_C2 ? "C2" : kOpNames[g.op];
+      const char* name = g.op == OP_C1 ? "C1" : g.op == OP_C2 ? "C2" : g.op == OP_CHANNEL ? "CHANNEL" : kOpNames[g.op];
       ss << name << "(" << g.qb[0] << "," << g.qb[1] << "," << g.qb[2] << "," << g.qb[3] << "," << g.qb[4] << ","
          << g.theta << "," << g.phi << "," << g.lambda << ");" << std::endl;
     }

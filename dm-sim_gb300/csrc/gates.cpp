@@ -151,6 +151,8 @@ int gate_arity(int op) {
     case CX: case CZ: case CY: case SWAP: case CH: case CRX: case CRY: case CRZ: case CU1: case CU3:
     case RXX: case RZZ: case RYY: case OP_C2:
       return 2;
+    case OP_CHANNEL:
+      return 1;  // at least one; the record's nq says how many
     case CCX: case CSWAP: case RCCX:
       return 3;
     case RC3X: case C3X: case C3SQRTX:
@@ -162,7 +164,7 @@ int gate_arity(int op) {
   }
 }
 
-void decompose(const GateRec& gr, std::vector<Basic>& out) {
+void decompose(const GateRec& gr, std::vector<Basic>& out, const std::vector<Channel>* chans) {
   Emit e{out};
   const int q0 = (int)gr.qb[0], q1 = (int)gr.qb[1], q2 = (int)gr.qb[2], q3 = (int)gr.qb[3], q4 = (int)gr.qb[4];
   const double th = gr.theta, ph = gr.phi, la = gr.lambda;
@@ -252,6 +254,17 @@ void decompose(const GateRec& gr, std::vector<Basic>& out) {
       cplx m[4];
       for (int i = 0; i < 4; i++) m[i] = cplx(gr.m[2 * i], gr.m[2 * i + 1]);
       e.m1(OP_C1, q0, m[0], m[1], m[2], m[3]);
+      break;
+    }
+    case OP_CHANNEL: {
+      Basic g;
+      std::memset(&g, 0, sizeof g);
+      g.kind = BK_SUPER;
+      g.op = OP_CHANNEL;
+      g.q[0] = q0;
+      g.q[1] = gr.nq == 2 ? q1 : -1;
+      g.chan = chans ? &(*chans)[gr.chan] : nullptr;
+      out.push_back(g);
       break;
     }
     case OP_C2: {

@@ -66,6 +66,10 @@ static cudaError_t launch_k(const LaunchArgs& a, cudaStream_t s) {
     case CLS_RLIN:
       if (K == 1) return launch_one<T, 1, CLS_RLIN>(a, s);
       return cudaErrorInvalidValue;
+    case CLS_SUPER:
+      if (K == 1) return launch_one<T, 1, CLS_SUPER>(a, s);
+      if (K == 2) return launch_one<T, 2, CLS_SUPER>(a, s);
+      return cudaErrorInvalidValue;
     default: return cudaErrorInvalidValue;
   }
 }
@@ -104,6 +108,7 @@ static int occ_k(int cls) {
     case CLS_PHASE: return occ_one<T, K, CLS_PHASE>();
     case CLS_DENSE: return occ_one<T, K, CLS_DENSE>();
     case CLS_SPARSE: return occ_one<T, K, CLS_SPARSE>();
+    case CLS_SUPER: return K <= 1 ? occ_one<T, 1, CLS_SUPER>() : occ_one<T, 2, CLS_SUPER>();
     default: return occ_one<T, 1, CLS_RLIN>();
   }
 }

@@ -29,7 +29,8 @@ enum PassClass : int32_t {
   CLS_DENSE = 3,   // general U, applied ket side then bra side (dense rows)
   CLS_SPARSE = 4,  // general U with sparse rows (per-row column lists)
   CLS_RLIN = 5,    // real-linear 1-qubit map (DM-Sim's SRN gate), K = 1
-  CLS_COUNT = 6
+  CLS_SUPER = 6,   // general superoperator (a noise channel), K <= 2: 4^K x 4^K on the (ket, bra) sub-index
+  CLS_COUNT = 7
 };
 
 // Factor kinds of a monomial superoperator entry f[a][b].
@@ -62,6 +63,9 @@ struct PassOp {
   double rlin[16];                 // RLIN: ket 4x4 real map on (r0,i0,r1,i1)
   double rlinb[16];                // RLIN: bra 4x4 real map
   int8_t nnz[D], nnzb[D];          // SPARSE: nonzeros per row of U and of V
+  int8_t nnzmax, nnzbmax;          // SPARSE: largest row count of U and of V
+  // SUPER: S[(a*D+b)*D*D + (c*D+e)] maps entry (c, e) to entry (a, b)
+  double sre[K <= 2 ? D * D * D * D : 1], sim[K <= 2 ? D * D * D * D : 1];
   int8_t col[D * D], colb[D * D];  // SPARSE: column lists per row
   int8_t src[D], srcb[D];          // monomial: source index of row a of U / row b of V
   int8_t fk[D * D];                // monomial: factor kind of f[a][b]

@@ -138,6 +138,8 @@ struct PassTables {
   int8_t fk[D * D];
   int8_t src[D], srcb[D], nnz[D], nnzb[D];
   int8_t col[CLS == CLS_SPARSE ? D * D : 1], colb[CLS == CLS_SPARSE ? D * D : 1];
+  int nnzmax, nnzbmax;
+  T ssr[CLS == CLS_SUPER && K <= 2 ? D * D * D * D : 1], ssi[CLS == CLS_SUPER && K <= 2 ? D * D * D * D : 1];
 };
 
 template <typename T, int K, int CLS>
@@ -178,6 +180,10 @@ __device__ void load_tables(const PassDesc<K>* __restrict__ dp, PassTables<T, K,
     tb.nnz[tid] = dp->op.nnz[tid];
     tb.nnzb[tid] = dp->op.nnzb[tid];
   }
+  if (tid == 0) {
+    tb.nnzmax = dp->op.nnzmax;
+    tb.nnzbmax = dp->op.nnzbmax;
+  }
   for (int i = tid; i < D * D; i += blockDim.x) {
     tb.fk[i] = dp->op.fk[i];
     if (PassTables<T, K, CLS>::kMat) {
@@ -198,6 +204,12 @@ __device__ void load_tables(const PassDesc<K>* __restrict__ dp, PassTables<T, K,
   if (CLS == CLS_RLIN && tid < 16) {
     tb.rl[tid] = coef<T>(dp->op.rlin[tid]);
     tb.rl[16 + tid] = coef<T>(dp->op.rlinb[tid]);
+  }
+  if constexpr (CLS == CLS_SUPER && K <= 2) {
+    for (int i = tid; i < D * D * D * D; i += blockDim.x) {
+      tb.ssr[i] = coef<T>(dp->op.sre[i]);
+      tb.ssi[i] = coef<T>(dp->op.sim[i]);
+    }
   }
 }
 
@@ -240,7 +252,44 @@ __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeade
   }
   __syncthreads();
 
-  if (CLS == CLS_DENSE || CLS == CLS_SPARSE || CLS == CLS_RLIN) {
+  if constexpr (CLS == CLS_SUPER && K <= 2) {
+    // ---- channel: each group's 4^K entries (a, b) <- S (4^K x 4^K), one thread per group
+    constexpr int DD = D * D;
+    if (tid < G) {
+      int ls = 0;
+      for (int j = 0; j < g; j++) ls |= ((tid >> j) & 1) << h.freepos[j];
+      T xr[DD], xi[DD];
+#pragma unroll
+      for (int ab = 0; ab < DD; ab++) {
+        const int loc = ls + tb.lk[ab / D] + tb.lb[ab % D];
+        xr[ab] = sre[loc];
+        xi[ab] = sim[loc];
+      }
+#pragma unroll
+      for (int o = 0; o < DD; o++) {
+        T ar = 0, ai = 0;
+#pragma unroll
+        for (int j = 0; j < DD; j++) {
+          const T mr = tb.ssr[o * DD + j], mi = tb.ssi[o * DD + j];
+          ar = madd(mr, xr[j], ar);
+          ar = madd(-mi, xi[j], ar);
+          ai = madd(mr, xi[j], ai);
+          ai = madd(mi, xr[j], ai);
+        }
+        const int loc = ls + tb.lk[o / D] + tb.lb[o % D];
+        sre[loc] = ar;
+        sim[loc] = ai;
+      }
+    }
+    __syncthreads();
+    for (int e2 = tid; e2 < (tile >> 1); e2 += blockDim.x) {
+      const int e = e2 << 1;
+      const int run = e >> L;
+      const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
+      st2<T>(re + ga, *reinterpret_cast<const T2*>(sre + e));
+      st2<T>(im + ga, *reinterpret_cast<const T2*>(sim + e));
+    }
+  } else if (CLS == CLS_DENSE || CLS == CLS_SPARSE || CLS == CLS_RLIN) {
     // ---- ket step: column (., b, f) <- U column
     if (has_item) {
       const int b = r_item;
@@ -274,23 +323,26 @@ __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeade
           sre[cb + tb.lk[a]] = ar;
           sim[cb + tb.lk[a]] = ai;
         }
-      } else {  // SPARSE
+      } else {  // SPARSE: the rows advance together (2^K independent chains)
         T yr[D], yi[D];
 #pragma unroll
         for (int a = 0; a < D; a++) {
-          T ar = 0, ai = 0;
-          const int nz = tb.nnz[a];
-          for (int j = 0; j < nz; j++) {
-            const int c = tb.col[a * D + j];
-            const T ur = tb.ure[a * D + c], ui = tb.uim[a * D + c];
-            const T vr = sre[cb + tb.lk[c]], vi = sim[cb + tb.lk[c]];
-            ar = madd(ur, vr, ar);
-            ar = madd(-ui, vi, ar);
-            ai = madd(ur, vi, ai);
-            ai = madd(ui, vr, ai);
+          yr[a] = 0;
+          yi[a] = 0;
+        }
+        for (int j = 0; j < tb.nnzmax; j++) {
+#pragma unroll
+          for (int a = 0; a < D; a++) {
+            if (j < tb.nnz[a]) {
+              const int c = tb.col[a * D + j];
+              const T ur = tb.ure[a * D + c], ui = tb.uim[a * D + c];
+              const T vr = sre[cb + tb.lk[c]], vi = sim[cb + tb.lk[c]];
+              yr[a] = madd(ur, vr, yr[a]);
+              yr[a] = madd(-ui, vi, yr[a]);
+              yi[a] = madd(ur, vi, yi[a]);
+              yi[a] = madd(ui, vr, yi[a]);
+            }
           }
-          yr[a] = ar;
-          yi[a] = ai;
         }
 #pragma unroll
         for (int a = 0; a < D; a++) {
@@ -334,23 +386,26 @@ __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeade
           sre[ca + tb.lb[b]] = ar;
           sim[ca + tb.lb[b]] = ai;
         }
-      } else {  // SPARSE
+      } else {  // SPARSE: the rows advance together (2^K independent chains)
         T yr[D], yi[D];
 #pragma unroll
         for (int b = 0; b < D; b++) {
-          T ar = 0, ai = 0;
-          const int nz = tb.nnzb[b];
-          for (int j = 0; j < nz; j++) {
-            const int c = tb.colb[b * D + j];
-            const T mr = tb.vre[b * D + c], mi = tb.vim[b * D + c];
-            const T vr = sre[ca + tb.lb[c]], vi = sim[ca + tb.lb[c]];
-            ar = madd(mr, vr, ar);
-            ar = madd(-mi, vi, ar);
-            ai = madd(mr, vi, ai);
-            ai = madd(mi, vr, ai);
+          yr[b] = 0;
+          yi[b] = 0;
+        }
+        for (int j = 0; j < tb.nnzbmax; j++) {
+#pragma unroll
+          for (int b = 0; b < D; b++) {
+            if (j < tb.nnzb[b]) {
+              const int c = tb.colb[b * D + j];
+              const T mr = tb.vre[b * D + c], mi = tb.vim[b * D + c];
+              const T vr = sre[ca + tb.lb[c]], vi = sim[ca + tb.lb[c]];
+              yr[b] = madd(mr, vr, yr[b]);
+              yr[b] = madd(-mi, vi, yr[b]);
+              yi[b] = madd(mr, vi, yi[b]);
+              yi[b] = madd(mi, vr, yi[b]);
+            }
           }
-          yr[b] = ar;
-          yi[b] = ai;
         }
 #pragma unroll
         for (int b = 0; b < D; b++) {

@@ -47,11 +47,25 @@ void apply_basic(cplx* U, int K, const int* qs, const Basic& b) {
   }
 }
 
-int nq(const Basic& b) { return b.kind == BK_2Q ? 2 : 1; }
+int nq(const Basic& b) {
+  if (b.kind == BK_SUPER) return b.chan->K;
+  return b.kind == BK_2Q ? 2 : 1;
+}
 
 PassSpec single(const Basic& b) {
   PassSpec p;
   p.nbasic = 1;
+  if (b.kind == BK_SUPER) {
+    p.K = b.chan->K;
+    p.q[0] = b.q[0];
+    if (p.K == 2) p.q[1] = b.q[1];
+    p.super = true;
+    const int DD = 1 << (2 * p.K);
+    for (int i = 0; i < DD * DD; i++) p.U[i] = b.chan->S[i];
+    p.cls = CLS_SUPER;
+    p.nnz = DD * DD;
+    return p;
+  }
   if (b.kind == BK_RLIN) {
     p.K = 1;
     p.q[0] = b.q[0];
@@ -169,7 +183,7 @@ std::vector<PassSpec> plan_greedy(const std::vector<Basic>& basics, int maxk, in
     while (first < m && taken[first]) first++;
     if (first >= m) break;
     const Basic& b0 = basics[first];
-    if (b0.kind == BK_RLIN || nq(b0) > maxk) {  // real-linear gates are fusion barriers
+    if (b0.kind == BK_RLIN || b0.kind == BK_SUPER || nq(b0) > maxk) {  // real-linear maps and channels are barriers
       take(first);
       out.push_back(single(b0));
       continue;
@@ -196,7 +210,7 @@ std::vector<PassSpec> plan_greedy(const std::vector<Basic>& basics, int maxk, in
         if (taken[j]) continue;
         seen++;
         const Basic& b = basics[j];
-        if (b.kind == BK_RLIN || !is_front(j)) continue;
+        if (b.kind == BK_RLIN || b.kind == BK_SUPER || !is_front(j)) continue;
         int add = 0;
         for (int t = 0; t < nq(b); t++) {
           bool in = false;
@@ -256,6 +270,10 @@ double snap1(double x, double eps) {
 }  // namespace
 
 void classify(PassSpec& p, bool fused) {
+  if (p.super) {
+    p.cls = CLS_SUPER;
+    return;
+  }
   if (p.rlin) {
     p.cls = CLS_RLIN;
     p.nnz = 4;
@@ -375,6 +393,12 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
   }
   std::memcpy(op.rlin, p.rl, sizeof op.rlin);
   std::memcpy(op.rlinb, p.rlb, sizeof op.rlinb);
+  if (p.cls == CLS_SUPER && K <= 2) {
+    for (int i = 0; i < D * D * D * D; i++) {
+      op.sre[i] = p.U[i].real();
+      op.sim[i] = p.U[i].imag();
+    }
+  }
   int src[kMaxD], srcb[kMaxD];
   for (int a = 0; a < D; a++) {
     int j = 0;
@@ -389,6 +413,8 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
     op.nnzb[a] = (int8_t)jb;
     srcb[a] = jb > 0 ? op.colb[a * D] : a;
     op.srcb[a] = (int8_t)srcb[a];
+    op.nnzmax = std::max<int8_t>(op.nnzmax, op.nnz[a]);
+    op.nnzbmax = std::max<int8_t>(op.nnzbmax, op.nnzb[a]);
   }
   const bool mono = p.cls == CLS_MOVE || p.cls == CLS_SIGNED || p.cls == CLS_PHASE;
   for (int a = 0; a < D; a++)
@@ -430,7 +456,7 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
   for (int a = 0; a < D; a++)
     for (int b = 0; b < D; b++) {
       bool changed;
-      if (p.cls == CLS_RLIN) changed = true;
+      if (p.cls == CLS_RLIN || p.cls == CLS_SUPER) changed = true;
       else if (mono) changed = src[a] != a || srcb[b] != b || op.fk[a * D + b] != FK_ONE;
       else changed = !(row_identity(p.U, a) && row_identity(p.V, b));
       if (changed) st[run_of(a, b)] = 1;
@@ -439,7 +465,7 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
     for (int b = 0; b < D; b++) {
       if (!st[run_of(a, b)]) continue;
       ld[run_of(a, b)] = 1;
-      if (p.cls == CLS_RLIN) {
+      if (p.cls == CLS_RLIN || p.cls == CLS_SUPER) {
         for (int a2 = 0; a2 < D; a2++)
           for (int b2 = 0; b2 < D; b2++) ld[run_of(a2, b2)] = 1;
       } else if (mono) {
@@ -456,7 +482,7 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
   // included, so every run is loaded: an unloaded run would feed
   // uninitialised shared memory (possibly NaN, and 0*NaN = NaN) into stored
   // entries.  MOVE/SIGNED/PHASE/SPARSE read only the sources listed above.
-  if (p.cls == CLS_DENSE || p.cls == CLS_RLIN) std::fill(ld.begin(), ld.end(), 1);
+  if (p.cls == CLS_DENSE || p.cls == CLS_RLIN || p.cls == CLS_SUPER) std::fill(ld.begin(), ld.end(), 1);
   int nst = 0, nld = 0;
   for (int r = 0; r < (1 << h.mhi); r++) {
     if (st[r]) {

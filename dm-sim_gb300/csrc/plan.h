@@ -19,6 +19,7 @@ struct PassSpec {
   bool ket_only = false;
   bool transpose = false;      // not an operator: the in-place conjugate transpose of rho
   bool rlin = false;
+  bool super = false;          // U holds a channel's (4^K x 4^K) superoperator, K <= 2
   double rl[16], rlb[16];
   int cls = CLS_DENSE;
   int nbasic = 0;              // basic gates this pass replaces

@@ -23,7 +23,9 @@ OP_NAMES = ["U3", "U2", "U1", "CX", "ID", "X", "Y", "Z", "H", "S",
             "RC3X", "C3X", "C3SQRTX", "C4X", "R", "SRN", "W", "RYY"]
 OP = {n: i for i, n in enumerate(OP_NAMES)}
 
-CLASS_NAMES = ["MOVE", "SIGNED", "PHASE", "DENSE", "SPARSE", "RLIN"]
+CLASS_NAMES = ["MOVE", "SIGNED", "PHASE", "DENSE", "SPARSE", "RLIN", "SUPER"]
+NOISE = {"depolarizing": 0, "amplitude_damping": 1, "phase_damping": 2, "bit_flip": 3, "phase_flip": 4,
+         "depolarizing2": 5}
 
 
 class DMSimError(RuntimeError):
@@ -96,6 +98,8 @@ def lib():
         "dmsim_batch_get_dm": [H, u32, P(d), P(d)],
         "dmsim_batch_stats": [H, P(d)],
         "dmsim_batch_autotune": [H, P(d)],
+        "dmsim_append_channel": [H, u32, P(u32), u32, P(d)],
+        "dmsim_append_noise": [H, ctypes.c_int, P(u32), d],
         "dmsim_plan_inspect": [u32, P(ctypes.c_int32), P(u32), P(d), P(d), u32, ctypes.c_int, ctypes.c_int,
                                ctypes.c_int, P(d), u32, P(u32)],
     }
@@ -190,6 +194,23 @@ class Simulation:
         flat = np.empty(32)
         flat[0::2], flat[1::2] = m.real, m.imag
         self._check(lib().dmsim_append_c2(self._h, int(q1), int(q2), _dp(flat)))
+
+    def append_channel(self, qubits, kraus):
+        """rho -> sum_i K_i rho K_i^+ on 1 or 2 qubits (2-qubit matrices in the
+        C2 basis order, index 2*bit(qubits[0]) + bit(qubits[1]))."""
+        qs = list(qubits)
+        k = np.asarray(kraus, dtype=np.complex128).reshape(len(kraus), -1)
+        flat = np.empty(2 * k.size)
+        flat[0::2], flat[1::2] = k.real.ravel(), k.imag.ravel()
+        q = (ctypes.c_uint32 * 2)(*(qs + [0] * (2 - len(qs))))
+        self._check(lib().dmsim_append_channel(self._h, len(qs), q, len(k), _dp(flat)))
+
+    def append_noise(self, kind, qubits, p):
+        """A named channel: depolarizing, amplitude_damping, phase_damping,
+        bit_flip, phase_flip (one qubit) or depolarizing2 (two qubits)."""
+        qs = list(qubits)
+        q = (ctypes.c_uint32 * 2)(*(qs + [0] * (2 - len(qs))))
+        self._check(lib().dmsim_append_noise(self._h, NOISE[kind], q, float(p)))
 
     def extend(self, circuit):
         for g in circuit:

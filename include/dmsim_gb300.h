@@ -72,6 +72,22 @@ int dmsim_append_c1(dmsim_handle h, uint32_t q, const double m[8]);
 /* Arbitrary 2-qubit gate (README "C2"; C2_GATE :1028-1122): m = 4x4 complex,
  * row-major, re/im interleaved (32 doubles), basis index 2*bit(q1) + bit(q2). */
 int dmsim_append_c2(dmsim_handle h, uint32_t q1, uint32_t q2, const double m[32]);
+/* Noise channel (no counterpart in the reference, which has no noise):
+ * rho -> sum_i K_i rho K_i^+ on nq = 1 or 2 qubits q[0..nq-1]; kraus holds
+ * n_kraus (<= 16) matrices of 2^nq x 2^nq complex, row-major, re/im
+ * interleaved, 2-qubit ones in the C2 basis order (index 2*bit(q[0]) +
+ * bit(q[1])).  Applied as one superoperator pass; a fusion barrier. */
+int dmsim_append_channel(dmsim_handle h, uint32_t nq, const uint32_t q[2], uint32_t n_kraus, const double* kraus);
+enum dmsim_noise {
+  DMSIM_NOISE_DEPOLARIZING = 0,       /* rho -> (1-p) rho + p I/2 */
+  DMSIM_NOISE_AMPLITUDE_DAMPING = 1,  /* gamma = p */
+  DMSIM_NOISE_PHASE_DAMPING = 2,      /* lambda = p */
+  DMSIM_NOISE_BIT_FLIP = 3,           /* X with probability p */
+  DMSIM_NOISE_PHASE_FLIP = 4,         /* Z with probability p */
+  DMSIM_NOISE_DEPOLARIZING2 = 5       /* two qubits: rho -> (1-p) rho + p I/4 */
+};
+/* A named channel of strength p in [0, 1] on q[0] (and q[1] for the 2-qubit kind). */
+int dmsim_append_noise(dmsim_handle h, int kind, const uint32_t q[2], double p);
 /* upload() -- :345-377.  Plans the passes and copies them to the device once. */
 int dmsim_upload(dmsim_handle h);
 /* sim() -- :390-494, without the copy of rho to the host (dmsim_get_dm). */
