@@ -249,6 +249,11 @@ def extra_workload(args):
 
 
 def main():
+    # replicas under torchrun: one GPU per rank.  The engine links its own CUDA
+    # runtime, so the rank's device is chosen before any CUDA call, for both it
+    # and torch, by restricting the visible devices.
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1 and "LOCAL_RANK" in os.environ:
+        os.environ["CUDA_VISIBLE_DEVICES"] = os.environ["LOCAL_RANK"]
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
@@ -283,7 +288,7 @@ def main():
     if world > 1:
         # replicas only: every rank runs the same single-GPU workload on its own device
         import torch
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        torch.cuda.set_device(0)  # the only visible device of this rank
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
@@ -296,6 +301,7 @@ def main():
     fused.upload()
     upload_s = time.perf_counter() - t_up0
     npasses, nbasic = fused.plan_stats()
+    upload_bytes = fused.upload_bytes()
     for _ in range(args.warmup):
         fused.run()
     if world > 1:
@@ -380,7 +386,8 @@ def main():
         cpu = {"value": v, "unit": "s/circuit", "cores": threads, "kind": "port", "sample": sample}
 
     if rank == 0:
-        value = step_ms / 1e3
+        # whole-job aggregate: the world's ranks each ran one circuit per step
+        value = step_ms / 1e3 / world
         line = {
             "metric": f"{n}q mixed-gate circuit time, fused FP64 passes (plain gate-by-gate path beside it)",
             "value": value, "unit": "s/circuit", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -399,7 +406,7 @@ def main():
                          "peak_kind": peak_kind, "launches": dcount},
             "kernels": kernels,
             "e2e": {"value": float(np.mean(e2e)), "unit": "s/circuit",
-                    "h2d_bytes_per_step": int(npasses * 4096), "d2h_bytes_per_step": int(16 * N)},
+                    "h2d_bytes_per_step": int(upload_bytes), "d2h_bytes_per_step": int(16 * N)},
             "gpu_launches": int(npasses * args.steps),
             "clocks": clk,
             "upload_s": upload_s,

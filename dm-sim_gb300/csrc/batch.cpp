@@ -189,6 +189,7 @@ void upload(dmsim_batch* b) {
     if (rlin) throw BErr{DMSIM_ERR_UNSUPPORTED, "the batched sweep does not take SRN (run such circuits singly)"};
     if (b->mode == 0) plans[c] = plan_plain(basics);
     else if (b->planner == 1) {
+      std::lock_guard<std::mutex> lock(cost_model_mutex());
       CostModel& m = global_cost_model();
       if (!m.ready) throw BErr{DMSIM_ERR_STATE, "the learned planner needs a trained or loaded cost model"};
       std::string err;

@@ -37,6 +37,11 @@ CostModel& global_cost_model() {
   return m;
 }
 
+std::mutex& cost_model_mutex() {
+  static std::mutex mu;
+  return mu;
+}
+
 namespace {
 constexpr uint32_t kMagic = 0x434d4d44;  // "DMMC"
 constexpr uint32_t kVersion = 1;

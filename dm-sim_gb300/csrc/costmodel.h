@@ -2,6 +2,7 @@
 #pragma once
 #include <stdint.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -20,6 +21,8 @@ struct CostModel {
 };
 
 CostModel& global_cost_model();
+// Held while the process-wide model is trained, loaded, saved or read.
+std::mutex& cost_model_mutex();
 bool cost_model_save(const CostModel& m, const std::string& path);
 bool cost_model_load(CostModel& m, const std::string& path);
 // He-initialised weights from a seed.

@@ -206,6 +206,7 @@ std::vector<PassSpec> make_plan(dmsim_sim* s, const std::vector<Basic>& basics) 
   if (has_rlin) return plan_reference_order(basics);
   if (s->mode == 0) return plan_plain(basics);
   if (s->planner == 1) {
+    std::lock_guard<std::mutex> lock(cost_model_mutex());
     CostModel& m = global_cost_model();
     if (!m.ready) load_default_cost_model();
     if (!m.ready)
@@ -817,6 +818,13 @@ int dmsim_plan_stats(dmsim_handle s, uint32_t* n_passes, uint32_t* n_basic) {
   });
 }
 
+int dmsim_upload_bytes(dmsim_handle s, uint64_t* bytes) {
+  DM_TRY(s, {
+    if (!bytes) throw DmError{DMSIM_ERR_ARG, "null output"};
+    *bytes = (uint64_t)s->desc_bytes;
+  });
+}
+
 int dmsim_last_timings(dmsim_handle s, double out[3]) {
   DM_TRY(s, {
     if (!out) throw DmError{DMSIM_ERR_ARG, "null output"};
@@ -958,6 +966,7 @@ int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qu
     if (has_rlin) specs = plan_reference_order(basics);
     else if (mode == 0) specs = plan_plain(basics);
     else if (planner == 1) {
+      std::lock_guard<std::mutex> lock(cost_model_mutex());
       CostModel& m = global_cost_model();
       if (!m.ready) load_default_cost_model();
       if (!m.ready) return DMSIM_ERR_STATE;
@@ -1080,6 +1089,7 @@ int dmsim_cost_train(const double* feats, const double* ms, uint32_t count, uint
   std::vector<float> X((size_t)count * kMlpIn), Y(count);
   for (size_t i = 0; i < X.size(); i++) X[i] = (float)feats[i];
   for (uint32_t i = 0; i < count; i++) Y[i] = (float)ms[i];
+  std::lock_guard<std::mutex> lock(cost_model_mutex());
   CostModel& m = global_cost_model();
   cost_model_init(m, seed);
   float l[2] = {0, 0};
@@ -1097,6 +1107,7 @@ int dmsim_cost_train(const double* feats, const double* ms, uint32_t count, uint
 
 int dmsim_cost_predict(const double* feats, uint32_t count, double* out_ms) {
   if (!feats || !out_ms) return DMSIM_ERR_ARG;
+  std::lock_guard<std::mutex> lock(cost_model_mutex());
   CostModel& m = global_cost_model();
   if (!m.ready) load_default_cost_model();
   if (!m.ready) return DMSIM_ERR_STATE;
@@ -1109,12 +1120,14 @@ int dmsim_cost_predict(const double* feats, uint32_t count, double* out_ms) {
 }
 
 int dmsim_cost_save(const char* path) {
+  std::lock_guard<std::mutex> lock(cost_model_mutex());
   if (!path || !global_cost_model().ready) return DMSIM_ERR_STATE;
   return cost_model_save(global_cost_model(), path) ? DMSIM_OK : DMSIM_ERR_ARG;
 }
 
 int dmsim_cost_load(const char* path) {
   if (!path) return DMSIM_ERR_ARG;
+  std::lock_guard<std::mutex> lock(cost_model_mutex());
   return cost_model_load(global_cost_model(), path) ? DMSIM_OK : DMSIM_ERR_ARG;
 }
 

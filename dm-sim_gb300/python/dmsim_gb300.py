@@ -71,6 +71,7 @@ def lib():
         "dmsim_n_gates": [H, P(u32)],
         "dmsim_plan_stats": [H, P(u32), P(u32)],
         "dmsim_last_timings": [H, P(d)],
+        "dmsim_upload_bytes": [H, P(u64)],
         "dmsim_pass_records": [H, P(d), u32, P(u32)],
         "dmsim_pure_metrics": [H, P(d), P(d), P(d)],
         "dmsim_pure_metrics_noalloc": [H, P(d), P(d), P(d)],
@@ -281,6 +282,11 @@ class Simulation:
         a, b = ctypes.c_uint32(), ctypes.c_uint32()
         self._check(lib().dmsim_plan_stats(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+    def upload_bytes(self):
+        v = ctypes.c_uint64()
+        self._check(lib().dmsim_upload_bytes(self._h, ctypes.byref(v)))
+        return v.value
 
     def last_timings(self):
         o = np.zeros(3)

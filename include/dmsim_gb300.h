@@ -115,6 +115,8 @@ int dmsim_n_qubits(dmsim_handle h, uint32_t* n);
 int dmsim_n_gates(dmsim_handle h, uint32_t* n);
 /* Passes of the uploaded plan and basic gates they replace. */
 int dmsim_plan_stats(dmsim_handle h, uint32_t* n_passes, uint32_t* n_basic);
+/* Bytes the last upload() copied to the device (the pass descriptors) */
+int dmsim_upload_bytes(dmsim_handle h, uint64_t* bytes);
 /* Timing of the last run: out[0] = ms, out[1] = passes, out[2] = bytes moved (algorithmic) */
 int dmsim_last_timings(dmsim_handle h, double out[3]);
 /* Per-pass records of the last recorded run (DMSIM_OPT_RECORD): for each pass
