@@ -349,6 +349,7 @@ def main():
     err = None
     plain_bytes = None
     plain_passes = None
+    plain_df64_s = plain_df64_bytes = plain_df64_err = None
     if not args.no_plain:
         plain = E.Simulation(n, mode="plain")
         plain.extend(circ)
@@ -360,6 +361,16 @@ def main():
         fused.reset_dm()
         fused.run()
         err = fused.compare(plain)
+        # the same plain method with its passes in double-float (opt-in): the
+        # plain path's HBM rate when the FP64 pipe is out of the way
+        pdf = E.Simulation(n, mode="plain", plain_arith="df64")
+        pdf.extend(circ)
+        pdf.upload()
+        pdf.run()
+        plain_df64_s = pdf.last_timings()["ms"] / 1e3
+        plain_df64_bytes = pdf.last_timings()["bytes"]
+        plain_df64_err = pdf.compare(plain)
+        pdf.close()
         plain.close()
 
     # ---- end to end through the C ABI with host buffers
@@ -401,6 +412,9 @@ def main():
             "fused_vs_plain_error": err,
             "hbm_GBps_fused_run": bytes_per_run / (step_ms * 1e-3) / 1e9,
             "hbm_GBps_plain_run": (plain_bytes / plain_s / 1e9) if plain_s else None,
+            "plain_df64_s": plain_df64_s,
+            "hbm_GBps_plain_df64_run": (plain_df64_bytes / plain_df64_s / 1e9) if plain_df64_s else None,
+            "plain_df64_vs_plain_error": plain_df64_err,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": hbm_peak,
                          "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": None,
                          "peak_kind": peak_kind, "launches": dcount},

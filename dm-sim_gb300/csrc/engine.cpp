@@ -72,6 +72,7 @@ struct dmsim_sim {
 
   int mode = 0, maxk = 4, planner = 0, record = 0, graph_on = 1, verbose = 0;
   int fused_arith = 1;  // fused FP64 runs compute in double-float (1) or FP64 (0)
+  int plain_arith = 0;  // plain FP64 runs compute in FP64 (0) or double-float (1)
   int renorm = 64;      // complex64: renormalise every renorm passes (0 = never)
   int arith = 0;        // arithmetic of the uploaded plan (kernels.h Arith)
   int64_t seed = -1;
@@ -189,11 +190,13 @@ void load_default_cost_model() {
 }
 
 // Arithmetic of a run: complex64 state -> FP32; a fused FP64 run ->
-// double-float unless the option asks for FP64; otherwise (the plain path, the
-// reference's order for SRN) FP64.
+// double-float unless the option asks for FP64; a plain run -> FP64 unless the
+// option asks for double-float; the reference's order for SRN -> FP64.
 int run_arith(const dmsim_sim* s, bool reference_order) {
   if (s->fp32) return AR_FP32;
-  if (s->mode == 1 && s->fused_arith && !reference_order) return AR_DF64;
+  if (reference_order) return AR_FP64;
+  if (s->mode == 1 && s->fused_arith) return AR_DF64;
+  if (s->mode == 0 && s->plain_arith) return AR_DF64;
   return AR_FP64;
 }
 
@@ -512,6 +515,10 @@ int dmsim_set_option(dmsim_handle s, int key, int64_t v) {
         if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set the fused arithmetic before upload()"};
         s->fused_arith = v != 0;
         break;
+      case DMSIM_OPT_PLAIN_ARITH:
+        if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set the plain arithmetic before upload()"};
+        s->plain_arith = v != 0;
+        break;
       case DMSIM_OPT_RENORM:
         if (v < 0) throw DmError{DMSIM_ERR_ARG, "renorm interval must be >= 0"};
         if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set the renormalisation interval before upload()"};
@@ -536,6 +543,7 @@ int dmsim_get_option(dmsim_handle s, int key, int64_t* v) {
       case DMSIM_OPT_VERBOSE: *v = s->verbose; break;
       case DMSIM_OPT_FUSED_ARITH: *v = s->fused_arith; break;
       case DMSIM_OPT_RENORM: *v = s->renorm; break;
+      case DMSIM_OPT_PLAIN_ARITH: *v = s->plain_arith; break;
       default: throw DmError{DMSIM_ERR_ARG, "unknown option"};
     }
   });

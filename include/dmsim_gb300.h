@@ -42,7 +42,8 @@ enum dmsim_option {
   DMSIM_OPT_GRAPH = 7,      /* 1 = replay uploaded circuits from a captured CUDA graph [1] */
   DMSIM_OPT_VERBOSE = 8,    /* 1 = print the reference's per-run timing banner [0] */
   DMSIM_OPT_FUSED_ARITH = 9, /* fused FP64 runs: 1 = double-float passes on the FP32 pipe [1], 0 = FP64 passes */
-  DMSIM_OPT_RENORM = 10      /* complex64: FP64 trace + Hermitian renormalisation every R passes and at the end [64]; 0 = off */
+  DMSIM_OPT_RENORM = 10,     /* complex64: FP64 trace + Hermitian renormalisation every R passes and at the end [64]; 0 = off */
+  DMSIM_OPT_PLAIN_ARITH = 11 /* plain FP64 runs: 0 = FP64 passes [0], 1 = double-float passes on the FP32 pipe */
 };
 
 /* Gate ids: the order of enum OP, src/dmsim_nvgpu_omp.cuh:42-48 (ABI). */

@@ -77,6 +77,20 @@ def test_srn_circuits_reference_order(engine, oracle, mode):
         assert maxerr(got, ref) <= 1e-12
 
 
+@pytest.mark.parametrize("n,seed", [(4, 0), (7, 1), (9, 2)])
+def test_plain_double_float_option(engine, oracle, n, seed):
+    """The plain method computed in double-float (DMSIM_OPT_PLAIN_ARITH) keeps
+    the plain path's 1e-12 bar."""
+    circ = W.random_circuit(n, 80, ops=NO_SRN, seed=800 + seed)
+    ref = oracle.dm_sim(n, circ)
+    with engine.Simulation(n, mode="plain", plain_arith="df64") as s:
+        s.extend(circ)
+        s.upload()
+        s.run()
+        got = s.get_dm()
+    assert maxerr(got, ref) <= 1e-12
+
+
 def test_c1_c2(engine, oracle):
     rng = np.random.default_rng(8)
 
