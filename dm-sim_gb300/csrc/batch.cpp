@@ -140,7 +140,7 @@ void build(dmsim_batch* b) {
   if (!blob.empty()) B_CUDA(cudaMemcpy(b->d_blob, blob.data(), blob.size(), cudaMemcpyHostToDevice));
   if (!ranges.empty())
     B_CUDA(cudaMemcpy(b->d_ranges, ranges.data(), ranges.size() * sizeof(BatchRange), cudaMemcpyHostToDevice));
-  b->grid = (unsigned)(b->sms * batch_blocks_per_sm());
+  b->grid = (unsigned)(b->sms * batch_blocks_per_sm(b->mode == 1));
   // one graph: reset -> queue -> epilogue
   BatchLaunch a;
   a.re = b->d_re;
@@ -159,6 +159,7 @@ void build(dmsim_batch* b) {
   a.zz = b->d_zz;
   a.grid = b->grid;
   a.spin_limit = 1u << 25;  // ~4 s of 128 ns naps before a wait gives up
+  a.df64_arith = b->mode == 1;  // fused batches compute in double-float, plain ones in FP64
   cudaGraph_t graph = nullptr;
   B_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = launch_batch(a, b->stream);
@@ -193,7 +194,7 @@ void upload(dmsim_batch* b) {
       CostModel& m = global_cost_model();
       if (!m.ready) throw BErr{DMSIM_ERR_STATE, "the learned planner needs a trained or loaded cost model"};
       std::string err;
-      plans[c] = plan_learned(basics, (int)b->nq[c], b->maxk, AR_FP64, m, nullptr, err);
+      plans[c] = plan_learned(basics, (int)b->nq[c], b->maxk, AR_DF64, m, nullptr, err);
       if (!err.empty()) throw BErr{DMSIM_ERR_CUDA, err};
     } else plans[c] = plan_greedy(basics, b->maxk);
     b->n_passes += plans[c].size();
@@ -393,6 +394,14 @@ int dmsim_batch_get_dm(dmsim_batch_handle b, uint32_t circuit, double* re, doubl
     const uint64_t N = 1ull << (2 * b->nq[circuit]);
     B_CUDA(cudaMemcpy(re, b->d_re + b->circs[circuit].state_off, N * sizeof(double), cudaMemcpyDeviceToHost));
     B_CUDA(cudaMemcpy(im, b->d_im + b->circs[circuit].state_off, N * sizeof(double), cudaMemcpyDeviceToHost));
+    if (b->mode == 1) {  // fused batches hold double-float pairs (hi, lo): widen on the host
+      for (double* p : {re, im})
+        for (uint64_t i = 0; i < N; i++) {
+          float hl[2];
+          std::memcpy(hl, p + i, sizeof hl);
+          p[i] = (double)hl[0] + (double)hl[1];
+        }
+    }
   });
 }
 

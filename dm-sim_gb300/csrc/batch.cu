@@ -54,7 +54,8 @@ __device__ void batch_dispatch_k(int cls, T* re, T* im, const unsigned char* blo
 
 }  // namespace
 
-__global__ void __launch_bounds__(kThreads) k_batch(double* re, double* im, const unsigned char* __restrict__ blob,
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_batch(T* re, T* im, const unsigned char* __restrict__ blob,
                                                     const BatchRange* __restrict__ ranges, int nranges,
                                                     unsigned long long nitems, unsigned long long* next,
                                                     unsigned* done, int* err, unsigned spin_limit) {
@@ -100,10 +101,10 @@ __global__ void __launch_bounds__(kThreads) k_batch(double* re, double* im, cons
     if (!s_skip) {
       const uint64_t t = s_item - R.item_begin;
       switch (R.K) {
-        case 1: batch_dispatch_k<double, 1>(R.cls, re, im, blob, R, r, t, smem_raw, &s_loaded); break;
-        case 2: batch_dispatch_k<double, 2>(R.cls, re, im, blob, R, r, t, smem_raw, &s_loaded); break;
-        case 3: batch_dispatch_k<double, 3>(R.cls, re, im, blob, R, r, t, smem_raw, &s_loaded); break;
-        default: batch_dispatch_k<double, 4>(R.cls, re, im, blob, R, r, t, smem_raw, &s_loaded); break;
+        case 1: batch_dispatch_k<T, 1>(R.cls, re, im, blob, R, r, t, smem_raw, &s_loaded); break;
+        case 2: batch_dispatch_k<T, 2>(R.cls, re, im, blob, R, r, t, smem_raw, &s_loaded); break;
+        case 3: batch_dispatch_k<T, 3>(R.cls, re, im, blob, R, r, t, smem_raw, &s_loaded); break;
+        default: batch_dispatch_k<T, 4>(R.cls, re, im, blob, R, r, t, smem_raw, &s_loaded); break;
       }
     }
     // publish the tile: every writer fences, then one count per tile
@@ -113,24 +114,29 @@ __global__ void __launch_bounds__(kThreads) k_batch(double* re, double* im, cons
   }
 }
 
-__global__ void k_batch_init(double* re, const BatchCircuit* __restrict__ circs, int ncirc) {
+template <typename T>
+__global__ void k_batch_init(T* re, const BatchCircuit* __restrict__ circs, int ncirc) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c < ncirc) re[circs[c].state_off] = 1.0;
+  if (c < ncirc) re[circs[c].state_off] = T(1);
 }
 
+__device__ __forceinline__ double to_double(double x) { return x; }
+__device__ __forceinline__ double to_double(df64 x) { return (double)x.hi + (double)x.lo; }
+
 // Per circuit (one block each): the diagonal of rho and <Z_i Z_{i+1}>.
-__global__ void __launch_bounds__(256) k_batch_epilogue(const double* __restrict__ re,
+template <typename T>
+__global__ void __launch_bounds__(256) k_batch_epilogue(const T* __restrict__ re,
                                                         const BatchCircuit* __restrict__ circs, double* __restrict__ diag,
                                                         double* __restrict__ zz) {
   const BatchCircuit C = circs[blockIdx.x];
   const int n = C.n;
   const uint64_t dim = 1ull << n;
-  const double* A = re + C.state_off;
+  const T* A = re + C.state_off;
   double acc[kBatchMaxQubits];
 #pragma unroll
   for (int i = 0; i < kBatchMaxQubits; i++) acc[i] = 0;
   for (uint64_t r = threadIdx.x; r < dim; r += blockDim.x) {
-    const double d = A[r * dim + r];
+    const double d = to_double(A[r * dim + r]);
     diag[C.diag_off + r] = d;
 #pragma unroll
     for (int i = 0; i < kBatchMaxQubits - 1; i++)
@@ -167,32 +173,43 @@ size_t batch_smem_bytes() {
   return m;
 }
 
-int batch_blocks_per_sm() {
+template <typename T>
+static int blocks_t() {
   const size_t smem = batch_smem_bytes();
-  cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(k_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch, kThreads, smem) != cudaSuccess) return 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<T>, kThreads, smem) != cudaSuccess) return 1;
   return nb > 0 ? nb : 1;
 }
 
-cudaError_t launch_batch(const BatchLaunch& a, cudaStream_t s) {
+int batch_blocks_per_sm(bool df64_arith) { return df64_arith ? blocks_t<df64>() : blocks_t<double>(); }
+
+template <typename T>
+static cudaError_t launch_t(const BatchLaunch& a, cudaStream_t s) {
   const size_t smem = batch_smem_bytes();
-  cudaError_t e = cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(k_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  // all-zero bytes are 0 in both FP64 and double-float
   e = cudaMemsetAsync(a.re, 0, a.total_entries * sizeof(double), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(a.im, 0, a.total_entries * sizeof(double), s);
   if (e != cudaSuccess) return e;
-  k_batch_init<<<(a.ncirc + 255) / 256, 256, 0, s>>>(a.re, a.circs, a.ncirc);
+  T* re = reinterpret_cast<T*>(a.re);
+  T* im = reinterpret_cast<T*>(a.im);
+  k_batch_init<T><<<(a.ncirc + 255) / 256, 256, 0, s>>>(re, a.circs, a.ncirc);
   e = cudaMemsetAsync(a.next, 0, sizeof(unsigned long long), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(a.done, 0, (size_t)a.nranges * sizeof(unsigned), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(a.err, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
-  k_batch<<<a.grid, kThreads, smem, s>>>(a.re, a.im, a.blob, a.ranges, a.nranges, a.nitems, a.next, a.done, a.err,
-                                         a.spin_limit);
+  k_batch<T><<<a.grid, kThreads, smem, s>>>(re, im, a.blob, a.ranges, a.nranges, a.nitems, a.next, a.done, a.err,
+                                            a.spin_limit);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_batch_epilogue<<<a.ncirc, 256, 0, s>>>(a.re, a.circs, a.diag, a.zz);
+  k_batch_epilogue<T><<<a.ncirc, 256, 0, s>>>(re, a.circs, a.diag, a.zz);
   return cudaGetLastError();
+}
+
+cudaError_t launch_batch(const BatchLaunch& a, cudaStream_t s) {
+  return a.df64_arith ? launch_t<df64>(a, s) : launch_t<double>(a, s);
 }
 
 }  // namespace dmg

@@ -39,10 +39,11 @@ struct BatchLaunch {
   double *diag, *zz;
   unsigned grid;
   unsigned spin_limit;
+  bool df64_arith;  // the states hold double-float pairs (fused batches)
 };
 
 size_t batch_smem_bytes();
-int batch_blocks_per_sm();
+int batch_blocks_per_sm(bool df64_arith);
 // memset states, rho_c = |0><0|, reset the queue, the work-queue kernel, the epilogue
 cudaError_t launch_batch(const BatchLaunch& a, cudaStream_t s);
 
