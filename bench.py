@@ -29,7 +29,8 @@ import numpy as np  # noqa: E402
 
 import dmsim_workloads as W  # noqa: E402
 
-CLASS_NAMES = ["MOVE", "SIGNED", "PHASE", "DENSE", "SPARSE", "RLIN"]
+CLASS_NAMES = {0: "MOVE", 1: "SIGNED", 2: "PHASE", 3: "DENSE", 4: "SPARSE", 5: "RLIN", 6: "SUPER", 16: "CONVERT",
+               17: "TRANSPOSE", 18: "RENORM"}
 
 
 def peaks():
@@ -139,6 +140,31 @@ def run_reference_arm(args, n, circ):
     print(json.dumps(line))
 
 
+def class_profile(sim, arith_name):
+    """One recorded (untimed-by-the-bench) run: per (K, class) launches, device
+    ms, share and HBM GB/s from the engine's per-pass CUDA events."""
+    import dmsim_gb300 as E
+    sim.set_option(E.OPT_RECORD, 1)
+    sim.run()
+    rec = sim.pass_records()
+    run_ms = sim.last_timings()["ms"]
+    sim.set_option(E.OPT_RECORD, 0)
+    groups = {}
+    for r in rec:
+        g = groups.setdefault((int(r[0]), int(r[1])), [0, 0.0, 0.0])
+        g[0] += 1
+        g[1] += r[6]
+        g[2] += r[7]
+    tot = sum(g[1] for g in groups.values()) or 1.0
+    kernels = {f"K{k}_{CLASS_NAMES[c]}": {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot, 4),
+                                          "GBps": round(v[2] / max(v[1], 1e-9) / 1e6, 1)}
+               for (k, c), v in sorted(groups.items(), key=lambda kv: -kv[1][1])}
+    (dK, dcls), (dcount, dms, dbytes) = max(groups.items(), key=lambda kv: kv[1][1])
+    dom = {"kernel": f"k_pass<{arith_name},{dK},{CLASS_NAMES[dcls]}>", "launches": dcount, "ms": dms,
+           "bytes": dbytes}
+    return kernels, dom, run_ms
+
+
 def timed_runs(sim, warmup, steps):
     for _ in range(warmup):
         sim.run()
@@ -206,13 +232,13 @@ def extra_workload(args):
         out["fused_passes"], out["basic_gates"] = fused.plan_stats()
         out["fused_GBps"] = fused.last_timings()["bytes"] / out["fused_s"] / 1e9
         fused.reset_dm()
-        fused.run()
+        out["fused_kernels"], _, _ = class_profile(fused, "df64")
         if not args.no_plain:
             plain = E.Simulation(n, mode="plain")
             plain.extend(circ)
             plain.upload()
-            plain.run()
-            out["plain_s"] = plain.last_timings()["ms"] / 1e3
+            out["plain_kernels"], _, pms = class_profile(plain, "double")
+            out["plain_s"] = pms / 1e3
             out["plain_GBps"] = plain.last_timings()["bytes"] / out["plain_s"] / 1e9
             out["speedup_fused_vs_plain"] = out["plain_s"] / out["fused_s"]
             out["fused_vs_plain_error"] = fused.compare(plain)
@@ -229,6 +255,8 @@ def extra_workload(args):
         out["clocks"] = clocks.stop()
         out["passes"], out["basic_gates"] = s.plan_stats()
         out["c64_GBps"] = s.last_timings()["bytes"] / out["c64_s"] / 1e9
+        s.reset_dm()
+        out["c64_kernels"], _, _ = class_profile(s, "float")
         d = s.get_diag()
         out["trace_fp64_sum"] = float(d.sum())
         s.close()
@@ -261,7 +289,7 @@ def main():
     ap.add_argument("--impl", default="engine")
     ap.add_argument("--n", type=int, default=14)
     ap.add_argument("--gates", type=int, default=2000)
-    ap.add_argument("--planner", default="greedy")
+    ap.add_argument("--planner", default="learned")
     ap.add_argument("--max-k", type=int, default=4)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -324,25 +352,19 @@ def main():
     bytes_per_run = fused.last_timings()["bytes"]
 
     # ---- per-pass profile of one fused run (untimed): the dominant kernel
-    fused.set_option(E.OPT_RECORD, 1)
-    fused.run()
-    rec = fused.pass_records()
-    fused.set_option(E.OPT_RECORD, 0)
-    groups = {}
-    for r in rec:
-        key = (int(r[0]), int(r[1]))
-        g = groups.setdefault(key, [0, 0.0, 0.0])
-        g[0] += 1
-        g[1] += r[6]
-        g[2] += r[7]
-    tot_ms = sum(g[1] for g in groups.values())
-    dom = max(groups.items(), key=lambda kv: kv[1][1])
-    (dK, dcls), (dcount, dms, dbytes) = dom
-    dom_name = f"k_pass<double,{dK},{CLASS_NAMES[dcls]}>"
-    achieved = dbytes / (dms * 1e-3) / 1e9
-    kernels = {f"K{k}_{CLASS_NAMES[c]}": {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot_ms, 4),
-                                          "GBps": round(v[2] / (v[1] * 1e-3) / 1e9, 1)}
-               for (k, c), v in sorted(groups.items(), key=lambda kv: -kv[1][1])}
+    kernels, dom, _ = class_profile(fused, "df64")
+    dom_name, dcount = dom["kernel"], dom["launches"]
+    achieved = dom["bytes"] / (dom["ms"] * 1e-3) / 1e9
+
+    # the fixed-width greedy planner on the same circuit (the learned planner's fallback)
+    greedy_s = greedy_passes = None
+    if args.planner == "learned" and not args.no_plain:
+        g = E.Simulation(n, mode="fused", max_k=args.max_k, planner="greedy")
+        g.extend(circ)
+        g.upload()
+        greedy_s = timed_runs(g, 1, 1) / 1e3
+        greedy_passes = g.plan_stats()[0]
+        g.close()
 
     # ---- plain path (the reference's method) and the fused-vs-plain error
     plain_s = None
@@ -350,12 +372,13 @@ def main():
     plain_bytes = None
     plain_passes = None
     plain_df64_s = plain_df64_bytes = plain_df64_err = None
+    plain_kernels = plain_df64_kernels = None
     if not args.no_plain:
         plain = E.Simulation(n, mode="plain")
         plain.extend(circ)
         plain.upload()
-        plain.run()
-        plain_s = plain.last_timings()["ms"] / 1e3
+        plain_kernels, _, plain_ms = class_profile(plain, "double")  # per-pass events cost ~us per 3 ms pass
+        plain_s = plain_ms / 1e3
         plain_bytes = plain.last_timings()["bytes"]
         plain_passes = plain.plan_stats()[0]
         fused.reset_dm()
@@ -366,8 +389,8 @@ def main():
         pdf = E.Simulation(n, mode="plain", plain_arith="df64")
         pdf.extend(circ)
         pdf.upload()
-        pdf.run()
-        plain_df64_s = pdf.last_timings()["ms"] / 1e3
+        plain_df64_kernels, _, pdf_ms = class_profile(pdf, "df64")
+        plain_df64_s = pdf_ms / 1e3
         plain_df64_bytes = pdf.last_timings()["bytes"]
         plain_df64_err = pdf.compare(plain)
         pdf.close()
@@ -400,21 +423,23 @@ def main():
         # whole-job aggregate: the world's ranks each ran one circuit per step
         value = step_ms / 1e3 / world
         line = {
-            "metric": f"{n}q mixed-gate circuit time, fused FP64 passes (plain gate-by-gate path beside it)",
+            "metric": "14/16q circuit time, learned-fused vs plain on 1 GB300 at <=1e-10 err; HBM %",
             "value": value, "unit": "s/circuit", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic (seeded circuits, state from |0..0><0..0|)",
-            "config": {"workload": f"table_mix n={n} gates={len(circ)} seed=2 (29-entry table, random distinct qubits)",
+            "dtype": "df64", "data": "synthetic (seeded circuits, state from |0..0><0..0|)",
+            "config": {"workload": f"{n}-qubit mixed-gate circuit: table_mix n={n} gates={len(circ)} seed=2 (29-entry table, random distinct qubits)",
                        "planner": args.planner, "max_k": args.max_k, "passes": npasses, "basic_gates": nbasic,
                        "l2": "inputs larger than L2 (rho = %.1f GB)" % (16.0 * N / 1e9), "parallelism": "replicas"},
-            "plain_s": plain_s, "plain_passes": plain_passes,
+            "state": "FP64 rho in and out; fused passes compute in double-float (FP32 hi+lo pairs)",
+            "plain_s": plain_s, "plain_passes": plain_passes, "plain_kernels": plain_kernels,
+            "greedy_s": greedy_s, "greedy_passes": greedy_passes,
             "speedup_fused_vs_plain": (plain_s / value) if plain_s else None,
             "fused_vs_plain_error": err,
             "hbm_GBps_fused_run": bytes_per_run / (step_ms * 1e-3) / 1e9,
             "hbm_GBps_plain_run": (plain_bytes / plain_s / 1e9) if plain_s else None,
             "plain_df64_s": plain_df64_s,
             "hbm_GBps_plain_df64_run": (plain_df64_bytes / plain_df64_s / 1e9) if plain_df64_s else None,
-            "plain_df64_vs_plain_error": plain_df64_err,
+            "plain_df64_vs_plain_error": plain_df64_err, "plain_df64_kernels": plain_df64_kernels,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": hbm_peak,
                          "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": None,
                          "peak_kind": peak_kind, "launches": dcount},

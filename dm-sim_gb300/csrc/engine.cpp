@@ -363,6 +363,9 @@ void run(dmsim_sim* s) {
       DM_CUDA(cudaEventElapsedTime(&pms, p.ev0, p.ev1));
       PassRecord r;
       r.feat = p.feat;
+      if (p.conv) r.feat.cls = kRecConvert;
+      else if (p.transpose) r.feat.cls = kRecTranspose;
+      else if (p.renorm) r.feat.cls = kRecRenorm;
       r.ms = pms;
       r.bytes = p.bytes;
       s->records.push_back(r);
@@ -1043,11 +1046,15 @@ void random_table_circuit(uint32_t n, uint32_t ngates, std::mt19937_64& rng, std
 
 int dmsim_cost_collect(uint32_t n, uint32_t n_circuits, uint32_t gates, uint64_t seed, int arith, double* feats,
                        double* ms, uint32_t cap, uint32_t* count) {
-  if (!count || n < 2 || n > 16 || arith < AR_FP64 || arith > AR_DF64 || arith == AR_FP32) return DMSIM_ERR_ARG;
+  if (!count || n < 2 || n > 16 || arith < AR_FP64 || arith > AR_DF64) return DMSIM_ERR_ARG;
   *count = 0;
   dmsim_handle h = nullptr;
   int st = dmsim_create(n, 1, &h);
-  if (st != DMSIM_OK) return st;
+  if (st == DMSIM_OK && arith == AR_FP32) st = dmsim_set_option(h, DMSIM_OPT_PRECISION, 1);  // complex64 state
+  if (st != DMSIM_OK) {
+    dmsim_destroy(h);
+    return st;
+  }
   std::mt19937_64 rng(seed);
   uint32_t got = 0;
   try {

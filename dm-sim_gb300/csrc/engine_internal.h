@@ -21,6 +21,9 @@ struct PassInfo {
   cudaEvent_t ev0, ev1; // per-pass timing (record mode)
 };
 
+// Passes that apply no gates (K = 0) report these class codes.
+constexpr int kRecConvert = 16, kRecTranspose = 17, kRecRenorm = 18;
+
 struct PassRecord {
   PassFeatures feat;
   double ms;

@@ -35,7 +35,7 @@ def main():
     feats, ms = [], []
     t0 = time.time()
     for i, n in enumerate(int(x) for x in args.sizes.split(",")):
-        for arith in (E.AR_DF64, E.AR_FP64):
+        for arith in (E.AR_DF64, E.AR_FP64, E.AR_FP32):
             f, m = E.cost_collect(n, n_circuits=args.circuits, gates=args.gates, seed=100 * args.seed + 10 * i + arith,
                                   arith=arith)
             feats.append(f)

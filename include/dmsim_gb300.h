@@ -121,7 +121,9 @@ int dmsim_upload_bytes(dmsim_handle h, uint64_t* bytes);
 /* Timing of the last run: out[0] = ms, out[1] = passes, out[2] = bytes moved (algorithmic) */
 int dmsim_last_timings(dmsim_handle h, double out[3]);
 /* Per-pass records of the last recorded run (DMSIM_OPT_RECORD): for each pass
- * 8 doubles {K, class, nnz, max_lo_bit, min_hi_bit, n, ms, bytes}. Returns count. */
+ * 8 doubles {K, class, nnz, max_lo_bit, min_hi_bit, n, ms, bytes}.  Passes
+ * that apply no gates have K = 0 and class 16 (FP64 <-> double-float
+ * conversion), 17 (conjugate transpose) or 18 (complex64 renormalisation). */
 int dmsim_pass_records(dmsim_handle h, double* out, uint32_t cap, uint32_t* count);
 /* Compare rho with a pure state psi (2^n complex, FP64) on the device:
  * out[0] = fidelity <psi|rho|psi>, out[1] = trace, out[2] = max |rho - psi psi^+|,
@@ -166,7 +168,8 @@ int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qu
  * touched fractions, target-bit positions, size, precision).
  * dmsim_cost_collect: run the engine's own random circuits (29-entry mixed
  * table, n qubits, mt19937_64 from seed) under several fusion plans on the
- * current GPU in the given arithmetic (0 FP64, 2 double-float), timing every
+ * current GPU in the given arithmetic (0 FP64, 1 FP32 on a complex64 state,
+ * 2 double-float), timing every
  * pass with CUDA events; writes up to cap samples and the total count.  dmsim_cost_train: fit the network on the GPU (Adam,
  * full batch, steps, lr, weights seeded by seed); loss[0..1] = first / last
  * mean squared error of standardised log time.  dmsim_cost_predict: GPU
