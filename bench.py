@@ -151,17 +151,17 @@ def class_profile(sim, arith_name):
     sim.set_option(E.OPT_RECORD, 0)
     groups = {}
     for r in rec:
-        g = groups.setdefault((int(r[0]), int(r[1])), [0, 0.0, 0.0])
+        g = groups.setdefault((int(r[0]), int(r[1]), int(r[8])), [0, 0.0, 0.0])
         g[0] += 1
         g[1] += r[6]
         g[2] += r[7]
     tot = sum(g[1] for g in groups.values()) or 1.0
-    kernels = {f"K{k}_{CLASS_NAMES[c]}": {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot, 4),
-                                          "GBps": round(v[2] / max(v[1], 1e-9) / 1e6, 1)}
-               for (k, c), v in sorted(groups.items(), key=lambda kv: -kv[1][1])}
-    (dK, dcls), (dcount, dms, dbytes) = max(groups.items(), key=lambda kv: kv[1][1])
-    dom = {"kernel": f"k_pass<{arith_name},{dK},{CLASS_NAMES[dcls]}>", "launches": dcount, "ms": dms,
-           "bytes": dbytes}
+    kernels = {f"K{k}_{CLASS_NAMES[c]}{'_TC' if tc else ''}": {
+        "launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot, 4),
+        "GBps": round(v[2] / max(v[1], 1e-9) / 1e6, 1)} for (k, c, tc), v in sorted(groups.items(), key=lambda kv: -kv[1][1])}
+    (dK, dcls, dtc), (dcount, dms, dbytes) = max(groups.items(), key=lambda kv: kv[1][1])
+    name = f"k_pass_tc<{dK}> ({CLASS_NAMES[dcls]} operator)" if dtc else f"k_pass<{arith_name},{dK},{CLASS_NAMES[dcls]}>"
+    dom = {"kernel": name, "launches": dcount, "ms": dms, "bytes": dbytes, "tc": bool(dtc)}
     return kernels, dom, run_ms
 
 

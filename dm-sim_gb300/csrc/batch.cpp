@@ -194,7 +194,7 @@ void upload(dmsim_batch* b) {
       CostModel& m = global_cost_model();
       if (!m.ready) throw BErr{DMSIM_ERR_STATE, "the learned planner needs a trained or loaded cost model"};
       std::string err;
-      plans[c] = plan_learned(basics, (int)b->nq[c], b->maxk, AR_DF64, m, nullptr, err);
+      plans[c] = plan_learned(basics, (int)b->nq[c], b->maxk, AR_DF64, false, m, nullptr, err);
       if (!err.empty()) throw BErr{DMSIM_ERR_CUDA, err};
     } else plans[c] = plan_greedy(basics, b->maxk);
     b->n_passes += plans[c].size();

@@ -30,6 +30,7 @@ void pass_features(const PassFeatures& f, float* x) {
   x[13] = (float)(nb / 34.0);                     // log2 of the entry count
   x[14] = f.arith == 1 ? 1.f : (f.arith == 2 ? 0.5f : 0.f);  // FP32 / double-float / FP64
   x[15] = (float)((f.nnz / (double)D) * f.ld_frac * std::ldexp(1.0, (int)nb - 28));  // arithmetic volume
+  x[16] = f.tc ? 1.f : 0.f;                       // on the tensor cores (cost independent of the density)
 }
 
 CostModel& global_cost_model() {
@@ -44,7 +45,7 @@ std::mutex& cost_model_mutex() {
 
 namespace {
 constexpr uint32_t kMagic = 0x434d4d44;  // "DMMC"
-constexpr uint32_t kVersion = 1;
+constexpr uint32_t kVersion = 2;
 }  // namespace
 
 bool cost_model_save(const CostModel& m, const std::string& path) {
@@ -62,13 +63,23 @@ bool cost_model_load(CostModel& m, const std::string& path) {
   FILE* f = fopen(path.c_str(), "rb");
   if (!f) return false;
   uint32_t hdr[4];
-  bool ok = fread(hdr, sizeof hdr, 1, f) == 1 && hdr[0] == kMagic && hdr[1] == kVersion && hdr[2] == (uint32_t)kMlpIn &&
-            hdr[3] == (uint32_t)kMlpParams;
+  bool ok = fread(hdr, sizeof hdr, 1, f) == 1 && hdr[0] == kMagic;
+  // version 1: 16 features (no tensor-core flag); its weights are widened
+  // with a zero column, so it scores every pass as an FP32-pipe pass
+  const uint32_t in = ok ? hdr[2] : 0;
+  ok = ok && ((hdr[1] == kVersion && in == (uint32_t)kMlpIn) || (hdr[1] == 1 && in == 16));
+  const uint32_t np = kMlpHidden * in + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden + kMlpHidden + 1;
+  ok = ok && hdr[3] == np;
   CostModel t;
+  std::vector<float> raw(ok ? np : 0);
   ok = ok && fread(&t.y_mean, sizeof(float), 1, f) == 1 && fread(&t.y_std, sizeof(float), 1, f) == 1;
-  ok = ok && fread(t.params, sizeof(float), kMlpParams, f) == (size_t)kMlpParams;
+  ok = ok && fread(raw.data(), sizeof(float), np, f) == (size_t)np;
   fclose(f);
   if (!ok) return false;
+  // W1[j][0..in) then the rest of the layout unchanged
+  for (int j = 0; j < kMlpHidden; j++)
+    for (int k = 0; k < kMlpIn; k++) t.params[j * kMlpIn + k] = k < (int)in ? raw[j * in + k] : 0.f;
+  std::copy(raw.begin() + kMlpHidden * in, raw.end(), t.params + kMlpHidden * kMlpIn);
   t.ready = true;
   m = t;
   return true;
@@ -208,8 +219,8 @@ bool cost_model_predict(const CostModel& m, const std::vector<float>& X, std::ve
   return true;
 }
 
-std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int maxk, int arith, const CostModel& m,
-                                   double* predicted_ms, std::string& err) {
+std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int maxk, int arith, bool tensor,
+                                   const CostModel& m, double* predicted_ms, std::string& err) {
   // candidate plans: the unfused plan, and greedy plans of every width up to
   // maxk under row-density caps
   std::vector<std::vector<PassSpec>> cands;
@@ -220,29 +231,58 @@ std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int 
       if (cap >= (1 << k) && cap != kMaxD) continue;  // no effect at this width
       cands.push_back(plan_greedy(basics, k, cap));
     }
-  // features of every pass of every candidate, one batched inference
+  // features of every pass of every candidate (and of its tensor-core
+  // variant where there is one), one batched inference
   std::vector<float> X;
-  std::vector<int> owner;
-  std::vector<unsigned char> buf(desc_size(kMaxK));
+  std::vector<int> owner, pass_of;
+  std::vector<char> is_tc;
+  std::vector<unsigned char> buf(std::max(desc_size(kMaxK), tc_desc_bytes(kMaxK)));
+  const bool tc_ok = tensor && arith == 2;  // double-float state only
   for (size_t c = 0; c < cands.size(); c++)
-    for (const PassSpec& p : cands[c]) {
-      PassFeatures f;
-      std::memset(&f, 0, sizeof f);
+    for (size_t i = 0; i < cands[c].size(); i++) {
+      const PassSpec& p = cands[c][i];
       if (p.transpose) continue;
-      build_desc(p, n, buf.data(), &f, nullptr, nullptr);
-      f.arith = arith;
-      float x[kMlpIn];
-      pass_features(f, x);
-      X.insert(X.end(), x, x + kMlpIn);
-      owner.push_back((int)c);
+      for (int v = 0; v < 2; v++) {
+        if (v == 1 && !(tc_ok && tc_eligible(p, n))) break;
+        PassFeatures f;
+        std::memset(&f, 0, sizeof f);
+        if (v == 0) build_desc(p, n, buf.data(), &f, nullptr, nullptr);
+        else build_tc_desc(p, n, buf.data(), &f, nullptr, nullptr);
+        f.arith = arith;
+        f.tc = v;
+        float x[kMlpIn];
+        pass_features(f, x);
+        X.insert(X.end(), x, x + kMlpIn);
+        owner.push_back((int)c);
+        pass_of.push_back((int)i);
+        is_tc.push_back((char)v);
+      }
     }
   std::vector<float> ms;
   if (!cost_model_predict(m, X, ms, err)) return {};
+  // per pass: the cheaper variant
+  std::vector<std::vector<float>> best_ms(cands.size());
+  std::vector<std::vector<char>> best_tc(cands.size());
+  for (size_t c = 0; c < cands.size(); c++) {
+    best_ms[c].assign(cands[c].size(), -1.f);
+    best_tc[c].assign(cands[c].size(), 0);
+  }
+  for (size_t r = 0; r < ms.size(); r++) {
+    float& b = best_ms[owner[r]][pass_of[r]];
+    if (b < 0 || ms[r] < b) {
+      b = ms[r];
+      best_tc[owner[r]][pass_of[r]] = is_tc[r];
+    }
+  }
   std::vector<double> tot(cands.size(), 0.0);
-  for (size_t i = 0; i < ms.size(); i++) tot[owner[i]] += ms[i];
+  for (size_t c = 0; c < cands.size(); c++)
+    for (float v : best_ms[c])
+      if (v > 0) tot[c] += v;
   const size_t best = (size_t)(std::min_element(tot.begin(), tot.end()) - tot.begin());
   if (predicted_ms) *predicted_ms = tot[best];
-  return cands[best];
+  std::vector<PassSpec> plan = cands[best];
+  for (size_t i = 0; i < plan.size(); i++) plan[i].tc = tc_ok ? best_tc[best][i] : -1;
+  return plan;
 }
 
 }  // namespace dmg

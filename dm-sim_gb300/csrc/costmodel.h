@@ -38,7 +38,10 @@ bool cost_model_predict(const CostModel& m, const std::vector<float>& X, std::ve
 // The learned planner: scores candidate plans (widths 1..maxk, row-density
 // caps, and the unfused plan) with the model, returns the cheapest.
 // arith: the arithmetic the chosen plan will run in (kernels.h Arith).
-std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int maxk, int arith, const CostModel& m,
+// With `tensor`, every pass that can run on the tensor cores is scored both
+// ways and keeps the cheaper (PassSpec::tc).
+std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int maxk, int arith, bool tensor,
+                                   const CostModel& m,
                                    double* predicted_ms, std::string& err);
 
 }  // namespace dmg

@@ -60,6 +60,7 @@ struct dmsim_sim {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double* d_diag = nullptr;
   double* d_acc = nullptr;
+  int* d_err = nullptr;  // set by a tensor pass whose bounded wait ran out
 
   std::vector<GateRec> circuit;
   std::vector<Channel> channels;  // superoperators of the circuit's noise channels
@@ -74,6 +75,7 @@ struct dmsim_sim {
   int fused_arith = 1;  // fused FP64 runs compute in double-float (1) or FP64 (0)
   int plain_arith = 0;  // plain FP64 runs compute in FP64 (0) or double-float (1)
   int renorm = 64;      // complex64: renormalise every renorm passes (0 = never)
+  int tensor = 0;       // double-float K = 3, 4 dense/sparse passes on the tensor cores
   int arith = 0;        // arithmetic of the uploaded plan (kernels.h Arith)
   int64_t seed = -1;
 
@@ -167,6 +169,8 @@ void enqueue_passes(dmsim_sim* s, bool timed) {
     a.arith = s->arith;
     a.grid = p.grid;
     a.tile_entries = p.tile_entries;
+    a.tc = p.tc;
+    a.err = s->d_err;
     if (timed) DM_CUDA(cudaEventRecord(p.ev0, s->stream));
     DM_CUDA(launch_pass(a, s->stream));
     if (timed) DM_CUDA(cudaEventRecord(p.ev1, s->stream));
@@ -216,7 +220,8 @@ std::vector<PassSpec> make_plan(dmsim_sim* s, const std::vector<Basic>& basics) 
       throw DmError{DMSIM_ERR_STATE, "the learned planner needs a cost model: train one (dmsim_cost_train) or load one "
                                      "(dmsim_cost_load, or set DMSIM_COST_MODEL)"};
     std::string err;
-    std::vector<PassSpec> p = plan_learned(basics, (int)s->n, s->maxk, run_arith(s, false), m, &s->predicted_ms, err);
+    std::vector<PassSpec> p =
+        plan_learned(basics, (int)s->n, s->maxk, run_arith(s, false), s->tensor != 0, m, &s->predicted_ms, err);
     if (!err.empty()) throw DmError{DMSIM_ERR_CUDA, "learned planner: " + err};
     return p;
   }
@@ -224,6 +229,17 @@ std::vector<PassSpec> make_plan(dmsim_sim* s, const std::vector<Basic>& basics) 
 }
 
 void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_basic, int arith);
+
+// A double-float pass of 3 or 4 qubits with at least kTcMinRowNnz nonzeros
+// per row of U runs on the tensor cores: their cost does not depend on the
+// density, the FP32-pipe kernel's grows with it.
+constexpr int kTcMinRowNnz = 3;
+bool use_tensor(const dmsim_sim* s, const PassSpec& p, int arith) {
+  if (!s->tensor || arith != AR_DF64 || !tc_eligible(p, (int)s->n)) return false;
+  if (s->tensor == 2) return true;    // every eligible pass (measurements)
+  if (p.tc >= 0) return p.tc != 0;    // the learned planner's choice
+  return p.nnz >= kTcMinRowNnz * (1 << p.K);
+}
 
 void upload(dmsim_sim* s) {
   if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "upload() called twice without clear_circuit() (:347-350)"};
@@ -247,10 +263,13 @@ void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_b
   s->arith = arith;
   // descriptors, 256-byte aligned, one host blob, one copy
   std::vector<size_t> offs;
+  std::vector<char> tcs;
   size_t total = 0;
   for (const PassSpec& p : specs) {
     offs.push_back(total);
-    if (!p.transpose) total += (desc_size(p.K) + 255) & ~(size_t)255;
+    const bool tc = use_tensor(s, p, arith);
+    tcs.push_back(tc);
+    if (!p.transpose) total += ((tc ? tc_desc_bytes(p.K) : desc_size(p.K)) + 255) & ~(size_t)255;
   }
   std::vector<unsigned char> blob(std::max<size_t>(total, 256));
   s->passes.clear();
@@ -276,7 +295,11 @@ void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_b
     }
     uint64_t ntiles = 0;
     int tile = 0;
-    const uint64_t entries = build_desc(specs[i], (int)s->n, blob.data() + offs[i], &pi.feat, &ntiles, &tile);
+    pi.tc = tcs[i] != 0;
+    const uint64_t entries =
+        pi.tc ? build_tc_desc(specs[i], (int)s->n, blob.data() + offs[i], &pi.feat, &ntiles, &tile)
+              : build_desc(specs[i], (int)s->n, blob.data() + offs[i], &pi.feat, &ntiles, &tile);
+    pi.feat.tc = pi.tc ? 1 : 0;
     pi.K = specs[i].K;
     pi.cls = specs[i].cls;
     pi.desc_off = offs[i];
@@ -284,7 +307,7 @@ void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_b
     pi.bytes = (double)entries * 2.0 * (double)esize(s);
     pi.nbasic = specs[i].nbasic;
     pi.feat.arith = arith;
-    const int bps = pass_blocks_per_sm(pi.K, pi.cls, arith);
+    const int bps = pi.tc ? tc_blocks_per_sm(pi.K) : pass_blocks_per_sm(pi.K, pi.cls, arith);
     const uint64_t cap = (uint64_t)s->sms * (uint64_t)bps;
     pi.grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, cap));
     s->passes.push_back(pi);
@@ -350,6 +373,16 @@ void run(dmsim_sim* s) {
   DM_CUDA(cudaEventRecord(s->ev1, s->stream));
   DM_CUDA(cudaEventSynchronize(s->ev1));
   DM_CUDA(cudaGetLastError());
+  bool any_tc = false;
+  for (const PassInfo& p : s->passes) any_tc |= p.tc;
+  if (any_tc) {
+    int flag = 0;
+    DM_CUDA(cudaMemcpy(&flag, s->d_err, sizeof flag, cudaMemcpyDeviceToHost));
+    if (flag) {
+      DM_CUDA(cudaMemset(s->d_err, 0, sizeof flag));
+      throw DmError{DMSIM_ERR_TIMEOUT, "a tensor-core pass did not see its MMAs complete in time"};
+    }
+  }
   float ms = 0;
   DM_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
   s->last_ms = ms;
@@ -453,6 +486,8 @@ int dmsim_create(uint32_t n_qubits, uint32_t n_gpus, dmsim_handle* out) {
     DM_CUDA(cudaEventCreate(&s->ev1));
     DM_CUDA(cudaMalloc(&s->d_diag, s->dim * sizeof(double)));
     DM_CUDA(cudaMalloc(&s->d_acc, 8 * sizeof(double)));
+    DM_CUDA(cudaMalloc(&s->d_err, 16));
+    DM_CUDA(cudaMemset(s->d_err, 0, 16));
     // rho is allocated on first use so that complex64 can be chosen first
     // (17 qubits fit only in complex64); FP64 up to 16 qubits is allocated now
     if (n_qubits <= 16) ensure_state(s);
@@ -472,6 +507,7 @@ int dmsim_destroy(dmsim_handle s) {
   free_state(s);
   if (s->d_diag) cudaFree(s->d_diag);
   if (s->d_acc) cudaFree(s->d_acc);
+  if (s->d_err) cudaFree(s->d_err);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -522,6 +558,11 @@ int dmsim_set_option(dmsim_handle s, int key, int64_t v) {
         if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set the plain arithmetic before upload()"};
         s->plain_arith = v != 0;
         break;
+      case DMSIM_OPT_TENSOR:
+        if (v < 0 || v > 2) throw DmError{DMSIM_ERR_ARG, "tensor must be 0, 1 or 2"};
+        if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set the tensor-core option before upload()"};
+        s->tensor = (int)v;
+        break;
       case DMSIM_OPT_RENORM:
         if (v < 0) throw DmError{DMSIM_ERR_ARG, "renorm interval must be >= 0"};
         if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set the renormalisation interval before upload()"};
@@ -547,6 +588,7 @@ int dmsim_get_option(dmsim_handle s, int key, int64_t* v) {
       case DMSIM_OPT_FUSED_ARITH: *v = s->fused_arith; break;
       case DMSIM_OPT_RENORM: *v = s->renorm; break;
       case DMSIM_OPT_PLAIN_ARITH: *v = s->plain_arith; break;
+      case DMSIM_OPT_TENSOR: *v = s->tensor; break;
       default: throw DmError{DMSIM_ERR_ARG, "unknown option"};
     }
   });
@@ -851,7 +893,7 @@ int dmsim_pass_records(dmsim_handle s, double* out, uint32_t cap, uint32_t* coun
     if (out)
       for (uint32_t i = 0; i < cap && i < s->records.size(); i++) {
         const PassRecord& r = s->records[i];
-        double* o = out + 8 * i;
+        double* o = out + DMSIM_PASS_RECORD * i;
         o[0] = r.feat.K;
         o[1] = r.feat.cls;
         o[2] = r.feat.nnz;
@@ -860,6 +902,7 @@ int dmsim_pass_records(dmsim_handle s, double* out, uint32_t cap, uint32_t* coun
         o[5] = r.feat.n;
         o[6] = r.ms;
         o[7] = r.bytes;
+        o[8] = r.feat.tc;
       }
   });
 }
@@ -982,7 +1025,7 @@ int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qu
       if (!m.ready) load_default_cost_model();
       if (!m.ready) return DMSIM_ERR_STATE;
       std::string err;
-      specs = plan_learned(basics, (int)n_qubits, max_k, AR_DF64, m, nullptr, err);
+      specs = plan_learned(basics, (int)n_qubits, max_k, AR_DF64, true, m, nullptr, err);
       if (!err.empty()) return DMSIM_ERR_CUDA;
     } else specs = plan_greedy(basics, max_k);
     if (npasses) *npasses = (uint32_t)specs.size();
@@ -1071,20 +1114,29 @@ int dmsim_cost_collect(uint32_t n, uint32_t n_circuits, uint32_t gates, uint64_t
         for (int rc : caps) {
           if (rc != kMaxD && rc >= (1 << k)) continue;
           std::vector<PassSpec> specs = k == 1 ? plan_plain(basics) : plan_greedy(basics, k, rc);
-          upload_specs(h, specs, (uint32_t)basics.size(), arith);
-          h->uploaded = true;
-          run(h);
-          for (const PassRecord& r : h->records) {
-            if (r.feat.K == 0) continue;  // format conversions are not passes
-            if (got < cap && feats && ms) {
-              float x[kMlpIn];
-              pass_features(r.feat, x);
-              for (int i = 0; i < kMlpIn; i++) feats[(size_t)got * kMlpIn + i] = x[i];
-              ms[got] = r.ms;
+          bool any_tc = false;
+          for (const PassSpec& p : specs) any_tc |= tc_eligible(p, (int)n);
+          // double-float plans are timed on the FP32 pipe and, where passes
+          // can run there, on the tensor cores
+          const int variants = (arith == AR_DF64 && any_tc) ? 2 : 1;
+          for (int v = 0; v < variants; v++) {
+            h->tensor = v == 1 ? 2 : 0;
+            upload_specs(h, specs, (uint32_t)basics.size(), arith);
+            h->uploaded = true;
+            run(h);
+            for (const PassRecord& r : h->records) {
+              if (r.feat.K == 0) continue;  // format conversions are not passes
+              if (v == 1 && !r.feat.tc) continue;  // already timed in the first variant
+              if (got < cap && feats && ms) {
+                float x[kMlpIn];
+                pass_features(r.feat, x);
+                for (int i = 0; i < kMlpIn; i++) feats[(size_t)got * kMlpIn + i] = x[i];
+                ms[got] = r.ms;
+              }
+              got++;
             }
-            got++;
+            clear_circuit(h);
           }
-          clear_circuit(h);
           h->circuit.clear();
           if (k == 1) break;
         }

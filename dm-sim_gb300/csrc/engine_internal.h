@@ -17,6 +17,7 @@ struct PassInfo {
   unsigned grid;
   double bytes;         // algorithmic bytes moved (reads + writes)
   int nbasic;
+  bool tc;              // runs on the tensor cores (tensor.cu)
   PassFeatures feat;
   cudaEvent_t ev0, ev1; // per-pass timing (record mode)
 };

@@ -17,12 +17,17 @@ struct LaunchArgs {
   int arith;           // Arith
   unsigned grid;       // blocks
   int tile_entries;    // G * 4^K
+  bool tc;             // tensor-core pass (desc is a TcDesc<K>; double-float state, K = 3, 4)
+  int* err;            // device flag set to 1 when a bounded wait of a tensor pass runs out
 };
 
 // Launch one pass on stream s.
 cudaError_t launch_pass(const LaunchArgs& a, cudaStream_t s);
 // Resident blocks per SM of the kernel instance for (K, cls, arithmetic).
 int pass_blocks_per_sm(int K, int cls, int arith);
+// Tensor-core passes (tensor.cu): launch, and resident blocks per SM.
+cudaError_t launch_pass_tc(const LaunchArgs& a, cudaStream_t s);
+int tc_blocks_per_sm(int K);
 // In place: FP64 entries <-> double-float pairs (the fused path's working format)
 cudaError_t launch_to_df64(void* re, void* im, uint64_t N, unsigned grid, cudaStream_t s);
 cudaError_t launch_from_df64(void* re, void* im, uint64_t N, unsigned grid, cudaStream_t s);

@@ -1,9 +1,9 @@
-// mlp.cu -- the pass cost model: a 16-32-32-1 ReLU network in FP32, with its
+// mlp.cu -- the pass cost model: a 17-32-32-1 ReLU network in FP32, with its
 // forward (inference), backward and Adam kernels.  The engine trains it on
 // per-pass timings it records on its own random circuits and uses it to score
 // candidate fusion plans.
 //
-// Parameter layout (kMlpParams floats): W1[32][16], b1[32], W2[32][32], b2[32],
+// Parameter layout (kMlpParams floats): W1[32][17], b1[32], W2[32][32], b2[32],
 // W3[32], b3.  Loss: mean squared error on log(ms).
 #include <cuda_runtime.h>
 #include <stdint.h>

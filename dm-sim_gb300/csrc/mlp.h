@@ -4,7 +4,7 @@
 
 namespace dmg {
 
-constexpr int kMlpIn = 16;
+constexpr int kMlpIn = 17;
 constexpr int kMlpHidden = 32;
 constexpr int kMlpParams = kMlpHidden * kMlpIn + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden + kMlpHidden + 1;
 

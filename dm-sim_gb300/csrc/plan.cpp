@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 
 namespace dmg {
 
@@ -518,6 +519,76 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
 }
 
 }  // namespace
+
+// Tensor-core pass: the geometry of the K-qubit pass with 2^(7-K) groups per
+// tile (128 columns per step), every run loaded, and the BF16 slices of the
+// real embeddings of U (ket) and V (bra).
+template <int K>
+uint64_t build_tc_k(const PassSpec& p, int n, TcDesc<K>* d, PassFeatures* feat, uint64_t* ntiles_out,
+                    int* tile_out) {
+  constexpr int D = 1 << K, R = 2 * D;
+  std::unique_ptr<PassDesc<K>> geo(new PassDesc<K>);
+  build_k<K>(p, n, geo.get(), feat, ntiles_out, tile_out, 7 - K);
+  std::memset(d, 0, sizeof(*d));
+  d->h = geo->h;
+  PassHeader& h = d->h;
+  const int nruns = 1 << h.mhi;
+  int nst = 0;
+  for (int r = 0; r < nruns; r++) {
+    h.ldmask[r >> 5] |= 1u << (r & 31);
+    nst += (h.stmask[r >> 5] >> (r & 31)) & 1;
+  }
+  if (feat) feat->ld_frac = 1.0;
+  for (int side = 0; side < 2; side++) {
+    const cplx* M = side ? p.V : p.U;
+    for (int row = 0; row < R; row++) {
+      double w[R];
+      const int a = row % D;
+      for (int k = 0; k < R; k++) {
+        const cplx m = M[a * D + (k % D)];
+        if (row < D) w[k] = k < D ? m.real() : -m.imag();
+        else w[k] = k < D ? m.imag() : m.real();
+      }
+      double mx = 0;
+      for (int k = 0; k < R; k++) mx = std::max(mx, std::fabs(w[k]));
+      int rexp = 0;
+      if (mx > 0) {
+        int e;
+        std::frexp(mx, &e);  // mx in [2^(e-1), 2^e): |w * 2^(7-e)| < 128
+        rexp = std::min(60, std::max(-60, 7 - e));
+      }
+      d->rexp[side][row] = rexp;
+      for (int k = 0; k < R; k++) {
+        double v = std::ldexp(w[k], rexp);
+        for (int j = 0; j < kTcSlices; j++) {
+          const double t = std::nearbyint(v);  // |t| <= 128: exact in BF16
+          const float tf = (float)t;
+          uint32_t bits;
+          std::memcpy(&bits, &tf, 4);
+          d->sl[side][j][tc_kmajor_offset(row, k, 16 * R) / 2] = (uint16_t)(bits >> 16);
+          v = (v - t) * 256.0;
+        }
+      }
+    }
+  }
+  const uint64_t runlen = 1ull << h.L;
+  return (uint64_t)(nst + nruns) * runlen * h.ntiles;
+}
+
+uint64_t build_tc_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries) {
+  if (p.K == 3) return build_tc_k<3>(p, n, static_cast<TcDesc<3>*>(out), f, ntiles, tile_entries);
+  return build_tc_k<4>(p, n, static_cast<TcDesc<4>*>(out), f, ntiles, tile_entries);
+}
+
+bool tc_eligible(const PassSpec& p, int n) {
+  if (p.transpose || p.rlin || p.super) return false;
+  if (p.K != 3 && p.K != 4) return false;
+  if (p.cls != CLS_DENSE && p.cls != CLS_SPARSE) return false;
+  // 7 - K free bits must fit below the tile: 2n - 2K >= 7 - K
+  return 2 * n - 2 * p.K >= 7 - p.K;
+}
+
+size_t tc_desc_bytes(int K) { return K == 3 ? sizeof(TcDesc<3>) : sizeof(TcDesc<4>); }
 
 uint64_t build_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries,
                     int g_cap) {

@@ -24,6 +24,7 @@ struct PassSpec {
   int cls = CLS_DENSE;
   int nbasic = 0;              // basic gates this pass replaces
   int nnz = 0;                 // nonzeros of U after snapping
+  int tc = -1;                 // tensor cores: -1 the engine's rule decides, 0 no, 1 yes (learned planner)
 };
 
 // Cost-model features of one pass (also recorded with its measured time).
@@ -34,6 +35,7 @@ struct PassFeatures {
   int min_hi_bit;   // lowest target bit at or above L (2n if none)
   int n;
   double ld_frac, st_frac;  // fraction of the state read / written
+  int tc;           // 1: the pass runs on the tensor cores
 };
 
 // Fusion planners.  Both keep program order on every qubit and only reorder
@@ -62,5 +64,11 @@ size_t desc_size(int K);
 // g_cap caps log2 of the groups per tile (the tile shape; 8 = the largest).
 uint64_t build_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries,
                     int g_cap = 8);
+// Tensor-core passes (dense K = 3, 4 operators on a double-float state):
+// whether a pass can run on the tensor cores, the size of its descriptor
+// (TcDesc<K>) and the descriptor itself.
+bool tc_eligible(const PassSpec& p, int n);
+size_t tc_desc_bytes(int K);
+uint64_t build_tc_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries);
 
 }  // namespace dmg

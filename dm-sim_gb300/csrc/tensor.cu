@@ -1,0 +1,365 @@
+// tensor.cu -- dense K = 3, 4 qubit passes on the tensor cores (tcgen05),
+// double-float state, FP64-level accuracy.
+//
+// A tile is 128 columns of one step: in the ket step column m = (b, f) holds
+// the 2^K entries rho[(., b, f)], in the bra step column m = (a, f) holds
+// rho[(a, ., f)].  Each column is split into kTcSlices BF16 slices on its own
+// power-of-two grid (x * 2^sc = sum_i s_i 256^-i, |s_i| <= 256); the host did
+// the same per row for the operator (W * 2^rexp = sum_j t_j 256^-j, |t_j| <=
+// 128).  One thread issues, per order o = 0..kTcSlices, the MMAs of every
+// slice pair i + j = o into the FP32 accumulator D_o (TMEM columns o*R ..):
+// each product is an integer below 2^15 and every D_o sum stays below 2^24,
+// so the tensor cores add exactly.  The threads then read the orders back and
+// recombine them in double-float.  Error per step (numpy emulation of this
+// arithmetic on random unitaries and columns): below 2^-46 of |W row|_2 |x|_2,
+// dominated by the 48-bit slicing of x and W.
+//
+// Threads: 256.  Thread (warp w, lane l) owns column m = 32*(w & 3) + l (the
+// TMEM lane its warp may read) and half hf = w >> 2 of it: hf = 0 slices and
+// produces the real parts, hf = 1 the imaginary parts.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels.h"
+#include "pass_device.cuh"
+#include "tc.cuh"
+
+namespace dmg {
+
+namespace {
+
+template <int K>
+struct TcShape {
+  static constexpr int D = 1 << K, R = 2 * D, G = 128 / D, TILE = 128 * D, S = kTcSlices;
+  static constexpr uint32_t SBO = 16 * R;           // bytes between 8-row groups of an R-wide K-major operand
+  static constexpr uint32_t A_BYTES = 128 * R * 2;  // one slice of the 128 columns
+  static constexpr uint32_t B_BYTES = R * R * 2;    // one slice of W or V
+  static constexpr int ORDERS = S + 1;  // slice-pair orders 0..S kept (the first dropped order is below 2^-48)
+  static constexpr uint32_t TMEM_COLS =
+      ORDERS * R <= 32 ? 32 : (ORDERS * R <= 64 ? 64 : (ORDERS * R <= 128 ? 128 : 256));
+  static_assert(ORDERS * R <= 256, "accumulators exceed the tensor-memory allocation");
+  static constexpr uint32_t IDESC = tc::idesc_bf16_f32(128, R);
+};
+
+template <int K>
+struct TcTables {
+  static constexpr int D = 1 << K, R = 2 * D;
+  uint64_t hioff[256];
+  uint32_t ldmask[8], stmask[8];
+  int lk[D], lb[D];
+  int rexp[2][R];
+  float colmax[2][128];
+  uint64_t bar;
+  uint32_t slot;
+};
+
+template <int K>
+constexpr size_t tc_smem_bytes() {
+  using S = TcShape<K>;
+  return (size_t)S::S * S::A_BYTES + 2 * (size_t)S::S * S::B_BYTES + 2 * (size_t)S::TILE * sizeof(df64) +
+         sizeof(TcTables<K>);
+}
+
+// The slices of x = h + l (double-float) on the grid 2^-lsc: s[i] (integers,
+// |s| <= 256) with x * 2^lsc = sum_i s[i] 256^-i + (residual < 256^-(S-1)).
+// The low part cannot reach slices 0..2 (|l| <= 2^-24 |h| and |h * 2^lsc| <
+// 128), so it is sliced from slice 3 on and added there.
+template <int S>
+__device__ __forceinline__ void slice_df(float h, float l, float sc, float sc24, float (&s)[S]) {
+  const float C = 12582912.f;  // 1.5 * 2^23: (v + C) - C rounds |v| < 2^22 to an integer
+  float v = __fmul_rn(h, sc);
+#pragma unroll
+  for (int i = 0; i < S; i++) {
+    const float t = __fsub_rn(__fadd_rn(v, C), C);
+    s[i] = t;
+    v = __fmul_rn(__fsub_rn(v, t), 256.f);
+  }
+  float u = __fmul_rn(l, sc24);
+#pragma unroll
+  for (int i = 3; i < S; i++) {
+    const float t = __fsub_rn(__fadd_rn(u, C), C);
+    s[i] = __fadd_rn(s[i], t);
+    u = __fmul_rn(__fsub_rn(u, t), 256.f);
+  }
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);  // exact: |a|, |b| <= 256 are integers
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+template <int D>
+__device__ __forceinline__ void tmem_ld_row(uint32_t taddr, float (&v)[D]) {
+  if constexpr (D == 16) tc::tmem_ld16(taddr, v);
+  else tc::tmem_ld8(taddr, v);
+}
+
+// One step (ket when !BRA) on the tile in shared memory.  Returns false (the
+// same on every thread) if the tensor core did not signal completion in time.
+template <int K, bool BRA>
+__device__ bool tc_step(df64* __restrict__ sre, df64* __restrict__ sim, unsigned char* sA, const unsigned char* sB,
+                        TcTables<K>& tb, uint32_t tmem, int lf_g, uint32_t& phase) {
+  using SH = TcShape<K>;
+  constexpr int D = SH::D, R = SH::R, S = SH::S, G = SH::G;
+  const int tid = threadIdx.x;
+  const int w = tid >> 5, l = tid & 31;
+  const int m = 32 * (w & 3) + l;
+  const int hf = w >> 2;
+  const int r = m / G;
+  const int base = lf_g + (BRA ? tb.lk[r] : tb.lb[r]);
+  const int* lc = BRA ? tb.lb : tb.lk;
+  df64* arr = hf ? sim : sre;
+
+  // ---- gather this half-column and agree on the column's grid
+  float xh[D], xl[D];
+  float mx = 0.f;
+#pragma unroll
+  for (int c = 0; c < D; c++) {
+    const df64 v = arr[base + lc[c]];
+    xh[c] = v.hi;
+    xl[c] = v.lo;
+    mx = fmaxf(mx, fabsf(v.hi));
+  }
+  tb.colmax[hf][m] = mx;
+  __syncthreads();
+  mx = fmaxf(tb.colmax[0][m], tb.colmax[1][m]);
+  // mx < 2^(eb-126): scale by 2^(133-eb) so that |x * sc| < 128.  Columns
+  // whose largest entry is below 2^-87 keep the scale 2^93 (their slices
+  // underflow towards 0; absolute error < 2^-87).
+  int eb = (__float_as_int(mx) >> 23) & 0xFF;
+  eb = max(eb, 40);
+  const int lsc = 133 - eb;
+  const float sc = __int_as_float((lsc + 127) << 23);
+  const float sc24 = __int_as_float((lsc + 24 + 127) << 23);
+
+  // ---- slices -> the A operand (row m, K index hf*D + c), 16 bytes per 8 values
+#pragma unroll
+  for (int c8 = 0; c8 < D; c8 += 8) {
+    uint32_t pk[S][4];
+#pragma unroll
+    for (int c = 0; c < 8; c += 2) {
+      float s0[S], s1[S];
+      slice_df<S>(xh[c8 + c], xl[c8 + c], sc, sc24, s0);
+      slice_df<S>(xh[c8 + c + 1], xl[c8 + c + 1], sc, sc24, s1);
+#pragma unroll
+      for (int i = 0; i < S; i++) pk[i][c >> 1] = pack_bf16(s0[i], s1[i]);
+    }
+    const uint32_t off = tc_kmajor_offset(m, hf * D + c8, SH::SBO);
+#pragma unroll
+    for (int i = 0; i < S; i++)
+      *reinterpret_cast<uint4*>(sA + i * SH::A_BYTES + off) = make_uint4(pk[i][0], pk[i][1], pk[i][2], pk[i][3]);
+  }
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+
+  // ---- one thread issues every slice-pair product, grouped by order
+  if (tid == 0) {
+    const uint32_t a0 = tc::smem_u32(sA);
+    const uint32_t b0 = tc::smem_u32(sB) + (BRA ? S * SH::B_BYTES : 0);
+#pragma unroll 1
+    for (int o = 0; o < SH::ORDERS; o++) {
+      uint32_t acc = 0;
+#pragma unroll 1
+      for (int i = (o < S ? 0 : o - S + 1); i <= o && i < S; i++) {
+        const int j = o - i;
+#pragma unroll
+        for (int kk = 0; kk < R / 16; kk++) {
+          const uint64_t ad = tc::smem_desc(a0 + i * SH::A_BYTES + kk * 256, tc::kLbo, SH::SBO);
+          const uint64_t bd = tc::smem_desc(b0 + j * SH::B_BYTES + kk * 256, tc::kLbo, SH::SBO);
+          tc::mma_bf16(tmem + o * R, ad, bd, SH::IDESC, acc);
+          acc = 1;
+        }
+      }
+    }
+    tc::mma_commit(&tb.bar);
+  }
+  const bool done = tc::mbar_wait_bounded(&tb.bar, phase, 1u << 24);
+  phase ^= 1u;
+  if (!__syncthreads_and(done)) return false;
+  tc::fence_after_sync();
+
+  // ---- recombine the orders of outputs n = hf*D + a (a < D) in double-float
+  const uint32_t trow = tmem + ((uint32_t)(32 * (w & 3)) << 16) + hf * D;
+  float lo[D], p3[D], p2[D], p1[D], p0[D];
+  {
+    float q[D];
+    tmem_ld_row<D>(trow + 6 * R, q);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int a = 0; a < D; a++) lo[a] = __fmul_rn(q[a], 0x1p-48f);
+    tmem_ld_row<D>(trow + 5 * R, q);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int a = 0; a < D; a++) lo[a] = __fmaf_rn(q[a], 0x1p-40f, lo[a]);
+    tmem_ld_row<D>(trow + 4 * R, q);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int a = 0; a < D; a++) lo[a] = __fmaf_rn(q[a], 0x1p-32f, lo[a]);
+  }
+  tmem_ld_row<D>(trow + 3 * R, p3);
+  tmem_ld_row<D>(trow + 2 * R, p2);
+  tmem_ld_row<D>(trow + 1 * R, p1);
+  tmem_ld_row<D>(trow, p0);
+  tc::tmem_wait_ld();
+#pragma unroll
+  for (int a = 0; a < D; a++) {
+    // orders 0..3 error-free (their sum spans more than 24 bits), 4..6 in lo
+    const df64 s1 = two_sum(p0[a], __fmul_rn(p1[a], 0x1p-8f));
+    const df64 s2 = two_sum(s1.hi, __fmul_rn(p2[a], 0x1p-16f));
+    const df64 s3 = two_sum(s2.hi, __fmul_rn(p3[a], 0x1p-24f));
+    const df64 y = fast_two_sum(s3.hi, __fadd_rn(__fadd_rn(__fadd_rn(s1.lo, s2.lo), s3.lo), lo[a]));
+    // y * 2^-(lsc + rexp): exact power-of-two scaling
+    const int fe = min(254, max(0, 127 - lsc - tb.rexp[BRA ? 1 : 0][hf * D + a]));  // 0: y is negligible
+    const float f = __int_as_float(fe << 23);
+    arr[base + lc[a]] = df64(__fmul_rn(y.hi, f), __fmul_rn(y.lo, f));
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  return true;
+}
+
+}  // namespace
+
+template <int K>
+__global__ void __launch_bounds__(kThreads, 2) k_pass_tc(df64* __restrict__ re, df64* __restrict__ im,
+                                                         const TcDesc<K>* __restrict__ dp, int* __restrict__ err) {
+  using SH = TcShape<K>;
+  constexpr int D = SH::D, S = SH::S;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* sA = smem;
+  unsigned char* sB = sA + S * SH::A_BYTES;
+  df64* sre = reinterpret_cast<df64*>(sB + 2 * S * SH::B_BYTES);
+  df64* sim = sre + SH::TILE;
+  TcTables<K>& tb = *reinterpret_cast<TcTables<K>*>(sim + SH::TILE);
+  const PassHeader& h = dp->h;
+  const int tid = threadIdx.x;
+
+  // ---- per-pass tables and the operator slices
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(&dp->sl[0][0][0]);
+    uint4* dst = reinterpret_cast<uint4*>(sB);
+    for (int i = tid; i < (int)(2 * S * SH::B_BYTES / 16); i += blockDim.x) dst[i] = src[i];
+  }
+  for (int r = tid; r < (1 << h.mhi); r += blockDim.x) {
+    uint64_t off = 0;
+    for (int j = 0; j < h.mhi; j++) off |= (uint64_t)((r >> j) & 1) << h.hipos[j];
+    tb.hioff[r] = off;
+  }
+  if (tid < 8) {
+    tb.ldmask[tid] = h.ldmask[tid];
+    tb.stmask[tid] = h.stmask[tid];
+  }
+  if (tid < D) {
+    int lk = 0, lb = 0;
+    for (int i = 0; i < K; i++) {
+      lk |= ((tid >> i) & 1) << h.lket[i];
+      lb |= ((tid >> i) & 1) << h.lbra[i];
+    }
+    tb.lk[tid] = lk;
+    tb.lb[tid] = lb;
+  }
+  if (tid < 2 * SH::R) tb.rexp[tid / SH::R][tid % SH::R] = dp->rexp[tid / SH::R][tid % SH::R];
+  if (tid < 32) {
+    tc::tmem_alloc(&tb.slot, SH::TMEM_COLS);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(&tb.bar, 1);
+    tc::mbar_fence_init();
+  }
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tb.slot;
+
+  // free-bit offset of this thread's group f = m mod G (the same in both steps)
+  int lf_g = 0;
+  {
+    const int m = 32 * ((tid >> 5) & 3) + (tid & 31);
+    const int f = m & (SH::G - 1);
+    for (int j = 0; j < h.g; j++) lf_g |= ((f >> j) & 1) << h.freepos[j];
+  }
+
+  const int L = h.L, runlen = 1 << L;
+  uint32_t phase = 0;
+  bool ok = true;
+  for (uint64_t t = blockIdx.x; t < h.ntiles; t += gridDim.x) {
+    uint64_t base = t << L;
+    for (int j = 0; j < h.mhi; j++) {
+      const int p = h.hipos[j];
+      base = ((base >> p) << (p + 1)) | (base & ((1ull << p) - 1));
+    }
+    // ---- load every run (the tensor cores multiply structural zeros too)
+    for (int e2 = tid; e2 < (SH::TILE >> 1); e2 += blockDim.x) {
+      const int e = e2 << 1;
+      const int run = e >> L;
+      const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
+      const df64x2 vr = ld2<df64>(re + ga);
+      const df64x2 vi = ld2<df64>(im + ga);
+      *reinterpret_cast<df64x2*>(sre + e) = vr;
+      *reinterpret_cast<df64x2*>(sim + e) = vi;
+    }
+    __syncthreads();
+    if (!tc_step<K, false>(sre, sim, sA, sB, tb, tmem, lf_g, phase) ||
+        !tc_step<K, true>(sre, sim, sA, sB, tb, tmem, lf_g, phase)) {
+      ok = false;
+      break;
+    }
+    // ---- store the runs the pass changes
+    for (int e2 = tid; e2 < (SH::TILE >> 1); e2 += blockDim.x) {
+      const int e = e2 << 1;
+      const int run = e >> L;
+      if (!((tb.stmask[run >> 5] >> (run & 31)) & 1)) continue;
+      const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
+      st2<df64>(re + ga, *reinterpret_cast<const df64x2*>(sre + e));
+      st2<df64>(im + ga, *reinterpret_cast<const df64x2*>(sim + e));
+    }
+    __syncthreads();
+  }
+  if (!ok && tid == 0) atomicExch(err, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (tid < 32) tc::tmem_dealloc(tmem, SH::TMEM_COLS);
+}
+
+template <int K>
+static cudaError_t launch_tc_k(const LaunchArgs& a, cudaStream_t s) {
+  constexpr size_t smem = tc_smem_bytes<K>();
+  static int configured = 0;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_pass_tc<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = 1;
+  }
+  k_pass_tc<K><<<a.grid, kThreads, smem, s>>>(static_cast<df64*>(a.re), static_cast<df64*>(a.im),
+                                               static_cast<const TcDesc<K>*>(a.desc), a.err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pass_tc(const LaunchArgs& a, cudaStream_t s) {
+  if (a.arith != AR_DF64 || !a.err) return cudaErrorInvalidValue;
+  if (a.K == 3) return launch_tc_k<3>(a, s);
+  if (a.K == 4) return launch_tc_k<4>(a, s);
+  return cudaErrorInvalidValue;
+}
+
+template <int K>
+static int tc_occ() {
+  constexpr size_t smem = tc_smem_bytes<K>();
+  cudaFuncSetAttribute(k_pass_tc<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pass_tc<K>, kThreads, smem) != cudaSuccess) return 1;
+  // TMEM: 512 columns per SM shared by the resident blocks
+  const int tmem_cap = 512 / (int)TcShape<K>::TMEM_COLS;
+  nb = nb < tmem_cap ? nb : tmem_cap;
+  return nb > 0 ? nb : 1;
+}
+
+int tc_blocks_per_sm(int K) { return K == 3 ? tc_occ<3>() : tc_occ<4>(); }
+
+}  // namespace dmg

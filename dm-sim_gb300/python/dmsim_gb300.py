@@ -14,8 +14,9 @@ LIB_PATH = os.path.normpath(os.path.join(_HERE, "..", "lib", "libdmsim_gb300.so"
 
 OK, ERR_ARG, ERR_STATE, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_UNSUPPORTED = range(7)
 (OPT_MODE, OPT_PRECISION, OPT_MAX_K, OPT_PLANNER, OPT_RECORD, OPT_SEED, OPT_GRAPH, OPT_VERBOSE, OPT_FUSED_ARITH,
- OPT_RENORM, OPT_PLAIN_ARITH) = range(1, 12)
+ OPT_RENORM, OPT_PLAIN_ARITH, OPT_TENSOR) = range(1, 13)
 AR_FP64, AR_FP32, AR_DF64 = 0, 1, 2
+PASS_RECORD = 9  # doubles per pass record: K, class, nnz, max_lo_bit, min_hi_bit, n, ms, bytes, tensor
 
 OP_NAMES = ["U3", "U2", "U1", "CX", "ID", "X", "Y", "Z", "H", "S",
             "SDG", "T", "TDG", "RX", "RY", "RZ", "CZ", "CY", "SWAP", "CH",
@@ -127,11 +128,13 @@ class Simulation:
 
     ``precision`` is "fp64" or "c64"; ``mode`` is "plain" (one pass per basic
     gate, the reference's method) or "fused"; ``planner`` is "greedy" or
-    "learned" (fused mode only).
+    "learned" (fused mode only); ``tensor`` runs double-float 3- and 4-qubit
+    dense passes on the tensor cores (True: where the planner's rule or cost
+    model picks them, "all" or 2: every eligible pass, False: none).
     """
 
     def __init__(self, n_qubits, n_gpus=1, precision="fp64", mode="plain", max_k=4, planner="greedy",
-                 graph=True, fused_arith="df64", renorm=64, plain_arith="fp64"):
+                 graph=True, fused_arith="df64", renorm=64, plain_arith="fp64", tensor=False):
         self._h = ctypes.c_void_p()
         self.n = int(n_qubits)
         st = lib().dmsim_create(self.n, int(n_gpus), ctypes.byref(self._h))
@@ -146,6 +149,7 @@ class Simulation:
             self.set_option(OPT_FUSED_ARITH, 1 if fused_arith == "df64" else 0)
             self.set_option(OPT_RENORM, int(renorm))
             self.set_option(OPT_PLAIN_ARITH, 1 if plain_arith == "df64" else 0)
+            self.set_option(OPT_TENSOR, 2 if tensor == "all" else int(tensor))
         except Exception:
             self.close()
             raise
@@ -297,7 +301,7 @@ class Simulation:
     def pass_records(self):
         cnt = ctypes.c_uint32()
         self._check(lib().dmsim_pass_records(self._h, None, 0, ctypes.byref(cnt)))
-        out = np.zeros((cnt.value, 8))
+        out = np.zeros((cnt.value, PASS_RECORD))
         if cnt.value:
             self._check(lib().dmsim_pass_records(self._h, _dp(out), cnt.value, ctypes.byref(cnt)))
         return out
@@ -408,8 +412,8 @@ class PinnedBuffer:
 
 
 # ---------------------------------------------------------------- cost model
-COST_FEATURES = 16
-MLP_PARAMS = 1633
+COST_FEATURES = 17
+MLP_PARAMS = 1665
 
 
 def _fp(a):

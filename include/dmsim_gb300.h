@@ -43,7 +43,10 @@ enum dmsim_option {
   DMSIM_OPT_VERBOSE = 8,    /* 1 = print the reference's per-run timing banner [0] */
   DMSIM_OPT_FUSED_ARITH = 9, /* fused FP64 runs: 1 = double-float passes on the FP32 pipe [1], 0 = FP64 passes */
   DMSIM_OPT_RENORM = 10,     /* complex64: FP64 trace + Hermitian renormalisation every R passes and at the end [64]; 0 = off */
-  DMSIM_OPT_PLAIN_ARITH = 11 /* plain FP64 runs: 0 = FP64 passes [0], 1 = double-float passes on the FP32 pipe */
+  DMSIM_OPT_PLAIN_ARITH = 11, /* plain FP64 runs: 0 = FP64 passes [0], 1 = double-float passes on the FP32 pipe */
+  DMSIM_OPT_TENSOR = 12       /* double-float runs: 1 = 3- and 4-qubit dense/sparse passes on the tensor cores
+                                 (BF16 slices, exact FP32 sums, double-float recombination), 0 = FP32 pipe [0],
+                                 2 = every eligible pass */
 };
 
 /* Gate ids: the order of enum OP, src/dmsim_nvgpu_omp.cuh:42-48 (ABI). */
@@ -121,9 +124,11 @@ int dmsim_upload_bytes(dmsim_handle h, uint64_t* bytes);
 /* Timing of the last run: out[0] = ms, out[1] = passes, out[2] = bytes moved (algorithmic) */
 int dmsim_last_timings(dmsim_handle h, double out[3]);
 /* Per-pass records of the last recorded run (DMSIM_OPT_RECORD): for each pass
- * 8 doubles {K, class, nnz, max_lo_bit, min_hi_bit, n, ms, bytes}.  Passes
+ * DMSIM_PASS_RECORD doubles {K, class, nnz, max_lo_bit, min_hi_bit, n, ms,
+ * bytes, tensor (1: ran on the tensor cores)}.  Passes
  * that apply no gates have K = 0 and class 16 (FP64 <-> double-float
  * conversion), 17 (conjugate transpose) or 18 (complex64 renormalisation). */
+#define DMSIM_PASS_RECORD 9
 int dmsim_pass_records(dmsim_handle h, double* out, uint32_t cap, uint32_t* count);
 /* Compare rho with a pure state psi (2^n complex, FP64) on the device:
  * out[0] = fidelity <psi|rho|psi>, out[1] = trace, out[2] = max |rho - psi psi^+|,
@@ -165,7 +170,7 @@ int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qu
                        double* out, uint32_t cap, uint32_t* npasses);
 /* ---- learned pass-time model (process-wide) --------------------------------
  * Features: DMSIM_COST_FEATURES doubles per pass (width, class, density,
- * touched fractions, target-bit positions, size, precision).
+ * touched fractions, target-bit positions, size, precision, tensor cores).
  * dmsim_cost_collect: run the engine's own random circuits (29-entry mixed
  * table, n qubits, mt19937_64 from seed) under several fusion plans on the
  * current GPU in the given arithmetic (0 FP64, 1 FP32 on a complex64 state,
@@ -174,7 +179,7 @@ int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qu
  * full batch, steps, lr, weights seeded by seed); loss[0..1] = first / last
  * mean squared error of standardised log time.  dmsim_cost_predict: GPU
  * inference, ms per sample.  save / load: the weights file. */
-#define DMSIM_COST_FEATURES 16
+#define DMSIM_COST_FEATURES 17
 int dmsim_cost_collect(uint32_t n, uint32_t n_circuits, uint32_t gates, uint64_t seed, int arith, double* feats,
                        double* ms, uint32_t cap, uint32_t* count);
 int dmsim_cost_train(const double* feats, const double* ms, uint32_t count, uint32_t steps, double lr, uint64_t seed,
@@ -184,7 +189,7 @@ int dmsim_cost_save(const char* path);
 int dmsim_cost_load(const char* path);
 /* The network's forward pass and its loss gradient on the GPU for given
  * parameters (DMSIM_MLP_PARAMS floats) -- the hooks the gradient check uses. */
-#define DMSIM_MLP_PARAMS 1633
+#define DMSIM_MLP_PARAMS 1665
 int dmsim_mlp_forward(const float* params, const float* X, uint32_t B, float* y);
 int dmsim_mlp_grad(const float* params, const float* X, const float* T, uint32_t B, float* grad, float* loss);
 /* Predicted run time of the uploaded plan (learned planner), ms */

@@ -6,7 +6,8 @@ import pytest
 
 import dmsim_workloads as W
 
-I, H = 16, 32
+I, H = 17, 32
+NP = H * I + H + H * H + H + H + 1  # network parameters
 
 
 def unpack(p):
@@ -49,12 +50,12 @@ def np_grad(p, X, T):
 def test_numpy_reference_gradient_is_a_gradient():
     """Finite differences pin the numpy reference itself (CPU)."""
     rng = np.random.default_rng(0)
-    p = rng.normal(size=1633) * 0.2
+    p = rng.normal(size=NP) * 0.2
     X = rng.random((7, I))
     T = rng.normal(size=7)
     g, _ = np_grad(p, X, T)
-    for idx in rng.choice(1633, 25, replace=False):
-        e = np.zeros(1633)
+    for idx in rng.choice(NP, 25, replace=False):
+        e = np.zeros(NP)
         e[idx] = 1e-6
         num = (np_grad(p + e, X, T)[1] - np_grad(p - e, X, T)[1]) / 2e-6
         assert abs(num - g[idx]) <= 1e-5 * max(1.0, abs(g[idx]))
@@ -63,7 +64,7 @@ def test_numpy_reference_gradient_is_a_gradient():
 @pytest.mark.gpu
 def test_gpu_forward_and_gradient_match_cpu(engine):
     rng = np.random.default_rng(1)
-    p = (rng.normal(size=1633) * 0.3).astype(np.float32)
+    p = (rng.normal(size=NP) * 0.3).astype(np.float32)
     X = rng.random((1000, I)).astype(np.float32)
     T = rng.normal(size=1000).astype(np.float32)
     y = engine.mlp_forward(p, X)
