@@ -223,7 +223,8 @@ def extra_workload(args):
     elif args.workload == "qft16":
         n = 16
         circ = W.qft_then_layers(n, 1000, seed=3)
-        fused = E.Simulation(n, mode="fused", max_k=args.max_k, planner=args.planner)
+        tensor = "all" if args.tensor == "all" else int(args.tensor)
+        fused = E.Simulation(n, mode="fused", max_k=args.max_k, planner=args.planner, tensor=tensor)
         fused.extend(circ)
         fused.upload()
         clocks.start()
@@ -291,6 +292,7 @@ def main():
     ap.add_argument("--gates", type=int, default=2000)
     ap.add_argument("--planner", default="learned")
     ap.add_argument("--max-k", type=int, default=4)
+    ap.add_argument("--tensor", default="1", help="tensor-core passes: 0 off, 1 planner's choice, all")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
@@ -323,7 +325,8 @@ def main():
     hbm_peak, peak_kind = peaks()
 
     # ---- fused path: the timed steps
-    fused = E.Simulation(n, mode="fused", max_k=args.max_k, planner=args.planner)
+    tensor = "all" if args.tensor == "all" else int(args.tensor)
+    fused = E.Simulation(n, mode="fused", max_k=args.max_k, planner=args.planner, tensor=tensor)
     t_up0 = time.perf_counter()
     fused.extend(circ)
     fused.upload()
@@ -359,7 +362,7 @@ def main():
     # the fixed-width greedy planner on the same circuit (the learned planner's fallback)
     greedy_s = greedy_passes = None
     if args.planner == "learned" and not args.no_plain:
-        g = E.Simulation(n, mode="fused", max_k=args.max_k, planner="greedy")
+        g = E.Simulation(n, mode="fused", max_k=args.max_k, planner="greedy", tensor=tensor)
         g.extend(circ)
         g.upload()
         greedy_s = timed_runs(g, 1, 1) / 1e3
@@ -428,7 +431,8 @@ def main():
             "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "df64", "data": "synthetic (seeded circuits, state from |0..0><0..0|)",
             "config": {"workload": f"{n}-qubit mixed-gate circuit: table_mix n={n} gates={len(circ)} seed=2 (29-entry table, random distinct qubits)",
-                       "planner": args.planner, "max_k": args.max_k, "passes": npasses, "basic_gates": nbasic,
+                       "planner": args.planner, "max_k": args.max_k, "tensor": args.tensor, "passes": npasses,
+                       "basic_gates": nbasic,
                        "l2": "inputs larger than L2 (rho = %.1f GB)" % (16.0 * N / 1e9), "parallelism": "replicas"},
             "state": "FP64 rho in and out; fused passes compute in double-float (FP32 hi+lo pairs)",
             "plain_s": plain_s, "plain_passes": plain_passes, "plain_kernels": plain_kernels,

@@ -35,6 +35,28 @@ __global__ void __launch_bounds__(kThreads) k_pass(T* __restrict__ re, T* __rest
   auto& tb = *reinterpret_cast<PassTables<T, K, CLS>*>(smem_raw + ((2 * (size_t)tile * sizeof(T) + 15) & ~(size_t)15));
   load_tables<T, K, CLS>(dp, tb);
   __syncthreads();
+  // Full-size tiles of narrow passes (2^(K-1) entry pairs per thread): the
+  // next tile's loads go out before the current tile is transformed.
+  constexpr int P = K >= 1 ? 1 << (K - 1) : 1;
+  if constexpr (K >= 1 && K <= 2) {
+    if (tile == 2 * kThreads * P) {
+      uint64_t t = blockIdx.x;
+      if (t >= h.ntiles) return;
+      TileRegs<T, P> x;
+      uint64_t base = tile_base(h, t);
+      load_regs<T, K, CLS, P>(re, im, h, tb, base, x);
+      for (; t < h.ntiles; t += gridDim.x) {
+        regs_to_smem<T, K, CLS, P>(h, tb, x, sre, sim);
+        __syncthreads();
+        const uint64_t tn = t + gridDim.x;
+        const uint64_t base_n = tn < h.ntiles ? tile_base(h, tn) : 0;
+        if (tn < h.ntiles) load_regs<T, K, CLS, P>(re, im, h, tb, base_n, x);
+        tile_body<T, K, CLS>(re, im, h, tb, base, sre, sim);
+        base = base_n;
+      }
+      return;
+    }
+  }
   for (uint64_t t = blockIdx.x; t < h.ntiles; t += gridDim.x) run_tile<T, K, CLS>(re, im, h, tb, t, sre, sim);
 }
 

@@ -241,32 +241,71 @@ __device__ void load_tables(const PassDesc<K>* __restrict__ dp, PassTables<T, K,
   }
 }
 
+// Global index of local entry 0 of tile t: zero bits inserted at the high
+// target positions into (t << L).
+__device__ __forceinline__ uint64_t tile_base(const PassHeader& h, uint64_t t) {
+  uint64_t base = t << h.L;
+  for (int j = 0; j < h.mhi; j++) {
+    const int p = h.hipos[j];
+    base = ((base >> p) << (p + 1)) | (base & ((1ull << p) - 1));
+  }
+  return base;
+}
+
+// Register staging of one tile's loads: thread tid holds entry pairs
+// tid + 256 i (i < P) -- the next tile's loads are issued before the current
+// tile is transformed, so their latency hides behind its arithmetic.
+template <typename T, int P>
+struct TileRegs {
+  typename Vec2<T>::type r[P], i[P];
+};
+
+template <typename T, int K, int CLS, int P>
+__device__ __forceinline__ void load_regs(const T* __restrict__ re, const T* __restrict__ im, const PassHeader& h,
+                                          const PassTables<T, K, CLS>& tb, uint64_t base, TileRegs<T, P>& x) {
+  const int runlen = 1 << h.L;
+#pragma unroll
+  for (int k = 0; k < P; k++) {
+    const int e = (threadIdx.x + k * kThreads) << 1;
+    const int run = e >> h.L;
+    if ((tb.ldmask[run >> 5] >> (run & 31)) & 1) {
+      const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
+      x.r[k] = ld2<T>(re + ga);
+      x.i[k] = ld2<T>(im + ga);
+    }
+  }
+}
+
+template <typename T, int K, int CLS, int P>
+__device__ __forceinline__ void regs_to_smem(const PassHeader& h, const PassTables<T, K, CLS>& tb,
+                                             const TileRegs<T, P>& x, T* __restrict__ sre, T* __restrict__ sim) {
+  using T2 = typename Vec2<T>::type;
+#pragma unroll
+  for (int k = 0; k < P; k++) {
+    const int e = (threadIdx.x + k * kThreads) << 1;
+    const int run = e >> h.L;
+    if ((tb.ldmask[run >> 5] >> (run & 31)) & 1) {
+      *reinterpret_cast<T2*>(sre + e) = x.r[k];
+      *reinterpret_cast<T2*>(sim + e) = x.i[k];
+    }
+  }
+}
+
+template <typename T, int K, int CLS>
+__device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHeader& h,
+                          const PassTables<T, K, CLS>& tb, uint64_t base, T* __restrict__ sre, T* __restrict__ sim);
+
 // One tile t of the pass on the state (re, im).  All threads of the block;
 // sre/sim hold G * 4^K entries each.  Ends synchronised.
 template <typename T, int K, int CLS>
 __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeader& h,
                          const PassTables<T, K, CLS>& tb, uint64_t t, T* __restrict__ sre, T* __restrict__ sim) {
-  constexpr int D = 1 << K;
   using T2 = typename Vec2<T>::type;
   const int tid = threadIdx.x;
-  const int L = h.L, mhi = h.mhi, g = h.g;
-  const int G = 1 << g;
-  const int tile = G * D * D;
+  const int L = h.L;
+  const int tile = (1 << h.g) * (1 << K) * (1 << K);
   const int runlen = 1 << L;
-  const bool has_item = tid < G * D;
-  int lf = 0;
-  {
-    const int f = tid & (G - 1);
-    for (int j = 0; j < g; j++) lf |= ((f >> j) & 1) << h.freepos[j];
-  }
-  const int r_item = tid >> g;  // b in the ket step, a in the bra step
-
-  // tile base: insert zero bits at the high target positions into (t << L)
-  uint64_t base = t << L;
-  for (int j = 0; j < mhi; j++) {
-    const int p = h.hipos[j];
-    base = ((base >> p) << (p + 1)) | (base & ((1ull << p) - 1));
-  }
+  const uint64_t base = tile_base(h, t);
   // ---- load touched runs (pairs of entries; runs are >= 2 long)
   for (int e2 = tid; e2 < (tile >> 1); e2 += blockDim.x) {
     const int e = e2 << 1;
@@ -279,6 +318,28 @@ __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeade
     *reinterpret_cast<T2*>(sim + e) = vi;
   }
   __syncthreads();
+  tile_body<T, K, CLS>(re, im, h, tb, base, sre, sim);
+}
+
+// The transform and the store of one tile whose touched runs are in shared
+// memory (after a barrier).  Ends synchronised.
+template <typename T, int K, int CLS>
+__device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHeader& h,
+                          const PassTables<T, K, CLS>& tb, uint64_t base, T* __restrict__ sre, T* __restrict__ sim) {
+  constexpr int D = 1 << K;
+  using T2 = typename Vec2<T>::type;
+  const int tid = threadIdx.x;
+  const int L = h.L, g = h.g;
+  const int G = 1 << g;
+  const int tile = G * D * D;
+  const int runlen = 1 << L;
+  const bool has_item = tid < G * D;
+  int lf = 0;
+  {
+    const int f = tid & (G - 1);
+    for (int j = 0; j < g; j++) lf |= ((f >> j) & 1) << h.freepos[j];
+  }
+  const int r_item = tid >> g;  // b in the ket step, a in the bra step
 
   if constexpr (CLS == CLS_SUPER && K <= 2) {
     // ---- channel: each group's 4^K entries (a, b) <- S (4^K x 4^K), one thread per group
