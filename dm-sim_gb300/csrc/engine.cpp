@@ -230,12 +230,12 @@ std::vector<PassSpec> make_plan(dmsim_sim* s, const std::vector<Basic>& basics) 
 
 void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_basic, int arith);
 
-// A double-float pass of 3 or 4 qubits with at least kTcMinRowNnz nonzeros
+// A double-float or complex64 pass of 3 or 4 qubits with at least kTcMinRowNnz nonzeros
 // per row of U runs on the tensor cores: their cost does not depend on the
 // density, the FP32-pipe kernel's grows with it.
 constexpr int kTcMinRowNnz = 3;
 bool use_tensor(const dmsim_sim* s, const PassSpec& p, int arith) {
-  if (!s->tensor || arith != AR_DF64 || !tc_eligible(p, (int)s->n)) return false;
+  if (!s->tensor || (arith != AR_DF64 && arith != AR_FP32) || !tc_eligible(p, (int)s->n)) return false;
   if (s->tensor == 2) return true;    // every eligible pass (measurements)
   if (p.tc >= 0) return p.tc != 0;    // the learned planner's choice
   return p.nnz >= kTcMinRowNnz * (1 << p.K);
@@ -307,7 +307,7 @@ void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_b
     pi.bytes = (double)entries * 2.0 * (double)esize(s);
     pi.nbasic = specs[i].nbasic;
     pi.feat.arith = arith;
-    const int bps = pi.tc ? tc_blocks_per_sm(pi.K) : pass_blocks_per_sm(pi.K, pi.cls, arith);
+    const int bps = pi.tc ? tc_blocks_per_sm(pi.K, arith) : pass_blocks_per_sm(pi.K, pi.cls, arith);
     const uint64_t cap = (uint64_t)s->sms * (uint64_t)bps;
     pi.grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, cap));
     s->passes.push_back(pi);
@@ -1118,7 +1118,7 @@ int dmsim_cost_collect(uint32_t n, uint32_t n_circuits, uint32_t gates, uint64_t
           for (const PassSpec& p : specs) any_tc |= tc_eligible(p, (int)n);
           // double-float plans are timed on the FP32 pipe and, where passes
           // can run there, on the tensor cores
-          const int variants = (arith == AR_DF64 && any_tc) ? 2 : 1;
+          const int variants = ((arith == AR_DF64 || arith == AR_FP32) && any_tc) ? 2 : 1;
           for (int v = 0; v < variants; v++) {
             h->tensor = v == 1 ? 2 : 0;
             upload_specs(h, specs, (uint32_t)basics.size(), arith);

@@ -17,7 +17,7 @@ struct LaunchArgs {
   int arith;           // Arith
   unsigned grid;       // blocks
   int tile_entries;    // G * 4^K
-  bool tc;             // tensor-core pass (desc is a TcDesc<K>; double-float state, K = 3, 4)
+  bool tc;             // tensor-core pass (desc is a TcDesc<K>; double-float or FP32 state, K = 3, 4)
   int* err;            // device flag set to 1 when a bounded wait of a tensor pass runs out
 };
 
@@ -27,7 +27,7 @@ cudaError_t launch_pass(const LaunchArgs& a, cudaStream_t s);
 int pass_blocks_per_sm(int K, int cls, int arith);
 // Tensor-core passes (tensor.cu): launch, and resident blocks per SM.
 cudaError_t launch_pass_tc(const LaunchArgs& a, cudaStream_t s);
-int tc_blocks_per_sm(int K);
+int tc_blocks_per_sm(int K, int arith);
 // In place: FP64 entries <-> double-float pairs (the fused path's working format)
 cudaError_t launch_to_df64(void* re, void* im, uint64_t N, unsigned grid, cudaStream_t s);
 cudaError_t launch_from_df64(void* re, void* im, uint64_t N, unsigned grid, cudaStream_t s);

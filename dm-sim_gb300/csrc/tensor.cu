@@ -1,5 +1,6 @@
-// tensor.cu -- dense K = 3, 4 qubit passes on the tensor cores (tcgen05),
-// double-float state, FP64-level accuracy.
+// tensor.cu -- dense K = 3, 4 qubit passes on the tensor cores (tcgen05):
+// double-float state with FP64-level accuracy (6 slices), or complex64 (FP32)
+// state with FP32-level accuracy (3 slices).
 //
 // A tile is 128 columns of one step: in the ket step column m = (b, f) holds
 // the 2^K entries rho[(., b, f)], in the bra step column m = (a, f) holds
@@ -21,6 +22,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "kernels.h"
 #include "pass_device.cuh"
 #include "tc.cuh"
@@ -29,13 +32,20 @@ namespace dmg {
 
 namespace {
 
-template <int K>
+// Slices per operand: 6 (48 bits) for a double-float state, 3 (24 bits) for
+// a complex64 (FP32) state.
+template <typename T> struct TcSlices { static constexpr int value = kTcSlices; };
+template <> struct TcSlices<float> { static constexpr int value = 3; };
+
+template <int K, typename T>
 struct TcShape {
-  static constexpr int D = 1 << K, R = 2 * D, G = 128 / D, TILE = 128 * D, S = kTcSlices;
+  static constexpr int D = 1 << K, R = 2 * D, G = 128 / D, TILE = 128 * D, S = TcSlices<T>::value;
   static constexpr uint32_t SBO = 16 * R;           // bytes between 8-row groups of an R-wide K-major operand
   static constexpr uint32_t A_BYTES = 128 * R * 2;  // one slice of the 128 columns
   static constexpr uint32_t B_BYTES = R * R * 2;    // one slice of W or V
-  static constexpr int ORDERS = S + 1;  // slice-pair orders 0..S kept (the first dropped order is below 2^-48)
+  // slice-pair orders kept: 0..S (double-float; the first dropped order is
+  // below 2^-48), 0..S (FP32: orders 0..3, below 2^-24 after that)
+  static constexpr int ORDERS = S + 1;
   static constexpr uint32_t TMEM_COLS =
       ORDERS * R <= 32 ? 32 : (ORDERS * R <= 64 ? 64 : (ORDERS * R <= 128 ? 128 : 256));
   static_assert(ORDERS * R <= 256, "accumulators exceed the tensor-memory allocation");
@@ -54,10 +64,10 @@ struct TcTables {
   uint32_t slot;
 };
 
-template <int K>
+template <int K, typename T>
 constexpr size_t tc_smem_bytes() {
-  using S = TcShape<K>;
-  return (size_t)S::S * S::A_BYTES + 2 * (size_t)S::S * S::B_BYTES + 2 * (size_t)S::TILE * sizeof(df64) +
+  using S = TcShape<K, T>;
+  return (size_t)S::S * S::A_BYTES + 2 * (size_t)S::S * S::B_BYTES + 2 * (size_t)S::TILE * sizeof(T) +
          sizeof(TcTables<K>);
 }
 
@@ -84,6 +94,19 @@ __device__ __forceinline__ void slice_df(float h, float l, float sc, float sc24,
   }
 }
 
+// The slices of an FP32 value on the grid 2^-lsc (|x * 2^lsc| < 128).
+template <int S>
+__device__ __forceinline__ void slice_f(float x, float sc, float (&s)[S]) {
+  const float C = 12582912.f;
+  float v = __fmul_rn(x, sc);
+#pragma unroll
+  for (int i = 0; i < S; i++) {
+    const float t = __fsub_rn(__fadd_rn(v, C), C);
+    s[i] = t;
+    v = __fmul_rn(__fsub_rn(v, t), 256.f);
+  }
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);  // exact: |a|, |b| <= 256 are integers
   return *reinterpret_cast<const uint32_t*>(&v);
@@ -97,11 +120,12 @@ __device__ __forceinline__ void tmem_ld_row(uint32_t taddr, float (&v)[D]) {
 
 // One step (ket when !BRA) on the tile in shared memory.  Returns false (the
 // same on every thread) if the tensor core did not signal completion in time.
-template <int K, bool BRA>
-__device__ bool tc_step(df64* __restrict__ sre, df64* __restrict__ sim, unsigned char* sA, const unsigned char* sB,
+template <int K, typename T, bool BRA>
+__device__ bool tc_step(T* __restrict__ sre, T* __restrict__ sim, unsigned char* sA, const unsigned char* sB,
                         TcTables<K>& tb, uint32_t tmem, int lf_g, uint32_t& phase) {
-  using SH = TcShape<K>;
+  using SH = TcShape<K, T>;
   constexpr int D = SH::D, R = SH::R, S = SH::S, G = SH::G;
+  constexpr bool DF = std::is_same<T, df64>::value;
   const int tid = threadIdx.x;
   const int w = tid >> 5, l = tid & 31;
   const int m = 32 * (w & 3) + l;
@@ -109,17 +133,21 @@ __device__ bool tc_step(df64* __restrict__ sre, df64* __restrict__ sim, unsigned
   const int r = m / G;
   const int base = lf_g + (BRA ? tb.lk[r] : tb.lb[r]);
   const int* lc = BRA ? tb.lb : tb.lk;
-  df64* arr = hf ? sim : sre;
+  T* arr = hf ? sim : sre;
 
   // ---- gather this half-column and agree on the column's grid
-  float xh[D], xl[D];
+  float xh[D], xl[DF ? D : 1];
   float mx = 0.f;
 #pragma unroll
   for (int c = 0; c < D; c++) {
-    const df64 v = arr[base + lc[c]];
-    xh[c] = v.hi;
-    xl[c] = v.lo;
-    mx = fmaxf(mx, fabsf(v.hi));
+    const T v = arr[base + lc[c]];
+    if constexpr (DF) {
+      xh[c] = v.hi;
+      xl[c] = v.lo;
+    } else {
+      xh[c] = v;
+    }
+    mx = fmaxf(mx, fabsf(xh[c]));
   }
   tb.colmax[hf][m] = mx;
   __syncthreads();
@@ -140,8 +168,13 @@ __device__ bool tc_step(df64* __restrict__ sre, df64* __restrict__ sim, unsigned
 #pragma unroll
     for (int c = 0; c < 8; c += 2) {
       float s0[S], s1[S];
-      slice_df<S>(xh[c8 + c], xl[c8 + c], sc, sc24, s0);
-      slice_df<S>(xh[c8 + c + 1], xl[c8 + c + 1], sc, sc24, s1);
+      if constexpr (DF) {
+        slice_df<S>(xh[c8 + c], xl[c8 + c], sc, sc24, s0);
+        slice_df<S>(xh[c8 + c + 1], xl[c8 + c + 1], sc, sc24, s1);
+      } else {
+        slice_f<S>(xh[c8 + c], sc, s0);
+        slice_f<S>(xh[c8 + c + 1], sc, s1);
+      }
 #pragma unroll
       for (int i = 0; i < S; i++) pk[i][c >> 1] = pack_bf16(s0[i], s1[i]);
     }
@@ -159,10 +192,10 @@ __device__ bool tc_step(df64* __restrict__ sre, df64* __restrict__ sim, unsigned
   if (tid == 0) {
     const uint32_t a0 = tc::smem_u32(sA);
     const uint32_t b0 = tc::smem_u32(sB) + (BRA ? S * SH::B_BYTES : 0);
-#pragma unroll 1
+#pragma unroll
     for (int o = 0; o < SH::ORDERS; o++) {
       uint32_t acc = 0;
-#pragma unroll 1
+#pragma unroll
       for (int i = (o < S ? 0 : o - S + 1); i <= o && i < S; i++) {
         const int j = o - i;
 #pragma unroll
@@ -181,40 +214,58 @@ __device__ bool tc_step(df64* __restrict__ sre, df64* __restrict__ sim, unsigned
   if (!__syncthreads_and(done)) return false;
   tc::fence_after_sync();
 
-  // ---- recombine the orders of outputs n = hf*D + a (a < D) in double-float
+  // ---- recombine the orders of outputs n = hf*D + a (a < D)
   const uint32_t trow = tmem + ((uint32_t)(32 * (w & 3)) << 16) + hf * D;
-  float lo[D], p3[D], p2[D], p1[D], p0[D];
-  {
-    float q[D];
-    tmem_ld_row<D>(trow + 6 * R, q);
+  if constexpr (DF) {
+    static_assert(S == 6, "the double-float recombination is written for orders 0..6");
+    float lo[D], p3[D], p2[D], p1[D], p0[D];
+    {
+      float q[D];
+      tmem_ld_row<D>(trow + 6 * R, q);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int a = 0; a < D; a++) lo[a] = __fmul_rn(q[a], 0x1p-48f);
+      tmem_ld_row<D>(trow + 5 * R, q);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int a = 0; a < D; a++) lo[a] = __fmaf_rn(q[a], 0x1p-40f, lo[a]);
+      tmem_ld_row<D>(trow + 4 * R, q);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int a = 0; a < D; a++) lo[a] = __fmaf_rn(q[a], 0x1p-32f, lo[a]);
+    }
+    tmem_ld_row<D>(trow + 3 * R, p3);
+    tmem_ld_row<D>(trow + 2 * R, p2);
+    tmem_ld_row<D>(trow + 1 * R, p1);
+    tmem_ld_row<D>(trow, p0);
     tc::tmem_wait_ld();
 #pragma unroll
-    for (int a = 0; a < D; a++) lo[a] = __fmul_rn(q[a], 0x1p-48f);
-    tmem_ld_row<D>(trow + 5 * R, q);
+    for (int a = 0; a < D; a++) {
+      // orders 0..3 error-free (their sum spans more than 24 bits), 4..6 in lo
+      const df64 s1 = two_sum(p0[a], __fmul_rn(p1[a], 0x1p-8f));
+      const df64 s2 = two_sum(s1.hi, __fmul_rn(p2[a], 0x1p-16f));
+      const df64 s3 = two_sum(s2.hi, __fmul_rn(p3[a], 0x1p-24f));
+      const df64 y = fast_two_sum(s3.hi, __fadd_rn(__fadd_rn(__fadd_rn(s1.lo, s2.lo), s3.lo), lo[a]));
+      // y * 2^-(lsc + rexp): exact power-of-two scaling
+      const int fe = min(254, max(0, 127 - lsc - tb.rexp[BRA ? 1 : 0][hf * D + a]));  // 0: y is negligible
+      const float f = __int_as_float(fe << 23);
+      arr[base + lc[a]] = df64(__fmul_rn(y.hi, f), __fmul_rn(y.lo, f));
+    }
+  } else {
+    static_assert(S == 3, "the FP32 recombination is written for orders 0..3");
+    float p3[D], p2[D], p1[D], p0[D];
+    tmem_ld_row<D>(trow + 3 * R, p3);
+    tmem_ld_row<D>(trow + 2 * R, p2);
+    tmem_ld_row<D>(trow + 1 * R, p1);
+    tmem_ld_row<D>(trow, p0);
     tc::tmem_wait_ld();
 #pragma unroll
-    for (int a = 0; a < D; a++) lo[a] = __fmaf_rn(q[a], 0x1p-40f, lo[a]);
-    tmem_ld_row<D>(trow + 4 * R, q);
-    tc::tmem_wait_ld();
-#pragma unroll
-    for (int a = 0; a < D; a++) lo[a] = __fmaf_rn(q[a], 0x1p-32f, lo[a]);
-  }
-  tmem_ld_row<D>(trow + 3 * R, p3);
-  tmem_ld_row<D>(trow + 2 * R, p2);
-  tmem_ld_row<D>(trow + 1 * R, p1);
-  tmem_ld_row<D>(trow, p0);
-  tc::tmem_wait_ld();
-#pragma unroll
-  for (int a = 0; a < D; a++) {
-    // orders 0..3 error-free (their sum spans more than 24 bits), 4..6 in lo
-    const df64 s1 = two_sum(p0[a], __fmul_rn(p1[a], 0x1p-8f));
-    const df64 s2 = two_sum(s1.hi, __fmul_rn(p2[a], 0x1p-16f));
-    const df64 s3 = two_sum(s2.hi, __fmul_rn(p3[a], 0x1p-24f));
-    const df64 y = fast_two_sum(s3.hi, __fadd_rn(__fadd_rn(__fadd_rn(s1.lo, s2.lo), s3.lo), lo[a]));
-    // y * 2^-(lsc + rexp): exact power-of-two scaling
-    const int fe = min(254, max(0, 127 - lsc - tb.rexp[BRA ? 1 : 0][hf * D + a]));  // 0: y is negligible
-    const float f = __int_as_float(fe << 23);
-    arr[base + lc[a]] = df64(__fmul_rn(y.hi, f), __fmul_rn(y.lo, f));
+    for (int a = 0; a < D; a++) {
+      float y = __fmaf_rn(p3[a], 0x1p-24f, __fmul_rn(p2[a], 0x1p-16f));
+      y = __fadd_rn(__fmaf_rn(p1[a], 0x1p-8f, y), p0[a]);
+      const int fe = min(254, max(0, 127 - lsc - tb.rexp[BRA ? 1 : 0][hf * D + a]));
+      arr[base + lc[a]] = __fmul_rn(y, __int_as_float(fe << 23));
+    }
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -223,25 +274,28 @@ __device__ bool tc_step(df64* __restrict__ sre, df64* __restrict__ sim, unsigned
 
 }  // namespace
 
-template <int K>
-__global__ void __launch_bounds__(kThreads, 2) k_pass_tc(df64* __restrict__ re, df64* __restrict__ im,
+template <int K, typename T>
+__global__ void __launch_bounds__(kThreads, 2) k_pass_tc(T* __restrict__ re, T* __restrict__ im,
                                                          const TcDesc<K>* __restrict__ dp, int* __restrict__ err) {
-  using SH = TcShape<K>;
+  using SH = TcShape<K, T>;
+  using T2 = typename Vec2<T>::type;
   constexpr int D = SH::D, S = SH::S;
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* sA = smem;
   unsigned char* sB = sA + S * SH::A_BYTES;
-  df64* sre = reinterpret_cast<df64*>(sB + 2 * S * SH::B_BYTES);
-  df64* sim = sre + SH::TILE;
+  T* sre = reinterpret_cast<T*>(sB + 2 * S * SH::B_BYTES);
+  T* sim = sre + SH::TILE;
   TcTables<K>& tb = *reinterpret_cast<TcTables<K>*>(sim + SH::TILE);
   const PassHeader& h = dp->h;
   const int tid = threadIdx.x;
 
-  // ---- per-pass tables and the operator slices
+  // ---- per-pass tables and the operator slices this state type uses
   {
-    const uint4* src = reinterpret_cast<const uint4*>(&dp->sl[0][0][0]);
-    uint4* dst = reinterpret_cast<uint4*>(sB);
-    for (int i = tid; i < (int)(2 * S * SH::B_BYTES / 16); i += blockDim.x) dst[i] = src[i];
+    constexpr int per_slice = SH::B_BYTES / 16;
+    for (int i = tid; i < 2 * S * per_slice; i += blockDim.x) {
+      const int side = i / (S * per_slice), rest = i % (S * per_slice);
+      reinterpret_cast<uint4*>(sB)[i] = reinterpret_cast<const uint4*>(&dp->sl[side][0][0])[rest];
+    }
   }
   for (int r = tid; r < (1 << h.mhi); r += blockDim.x) {
     uint64_t off = 0;
@@ -288,24 +342,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_pass_tc(df64* __restrict__ re, 
   uint32_t phase = 0;
   bool ok = true;
   for (uint64_t t = blockIdx.x; t < h.ntiles; t += gridDim.x) {
-    uint64_t base = t << L;
-    for (int j = 0; j < h.mhi; j++) {
-      const int p = h.hipos[j];
-      base = ((base >> p) << (p + 1)) | (base & ((1ull << p) - 1));
-    }
+    const uint64_t base = tile_base(h, t);
     // ---- load every run (the tensor cores multiply structural zeros too)
     for (int e2 = tid; e2 < (SH::TILE >> 1); e2 += blockDim.x) {
       const int e = e2 << 1;
       const int run = e >> L;
       const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
-      const df64x2 vr = ld2<df64>(re + ga);
-      const df64x2 vi = ld2<df64>(im + ga);
-      *reinterpret_cast<df64x2*>(sre + e) = vr;
-      *reinterpret_cast<df64x2*>(sim + e) = vi;
+      const T2 vr = ld2<T>(re + ga);
+      const T2 vi = ld2<T>(im + ga);
+      *reinterpret_cast<T2*>(sre + e) = vr;
+      *reinterpret_cast<T2*>(sim + e) = vi;
     }
     __syncthreads();
-    if (!tc_step<K, false>(sre, sim, sA, sB, tb, tmem, lf_g, phase) ||
-        !tc_step<K, true>(sre, sim, sA, sB, tb, tmem, lf_g, phase)) {
+    if (!tc_step<K, T, false>(sre, sim, sA, sB, tb, tmem, lf_g, phase) ||
+        !tc_step<K, T, true>(sre, sim, sA, sB, tb, tmem, lf_g, phase)) {
       ok = false;
       break;
     }
@@ -315,8 +365,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_pass_tc(df64* __restrict__ re, 
       const int run = e >> L;
       if (!((tb.stmask[run >> 5] >> (run & 31)) & 1)) continue;
       const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
-      st2<df64>(re + ga, *reinterpret_cast<const df64x2*>(sre + e));
-      st2<df64>(im + ga, *reinterpret_cast<const df64x2*>(sim + e));
+      st2<T>(re + ga, *reinterpret_cast<const T2*>(sre + e));
+      st2<T>(im + ga, *reinterpret_cast<const T2*>(sim + e));
     }
     __syncthreads();
   }
@@ -327,39 +377,42 @@ __global__ void __launch_bounds__(kThreads, 2) k_pass_tc(df64* __restrict__ re, 
   if (tid < 32) tc::tmem_dealloc(tmem, SH::TMEM_COLS);
 }
 
-template <int K>
+template <int K, typename T>
 static cudaError_t launch_tc_k(const LaunchArgs& a, cudaStream_t s) {
-  constexpr size_t smem = tc_smem_bytes<K>();
+  constexpr size_t smem = tc_smem_bytes<K, T>();
   static int configured = 0;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_pass_tc<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_pass_tc<K, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     configured = 1;
   }
-  k_pass_tc<K><<<a.grid, kThreads, smem, s>>>(static_cast<df64*>(a.re), static_cast<df64*>(a.im),
-                                               static_cast<const TcDesc<K>*>(a.desc), a.err);
+  k_pass_tc<K, T><<<a.grid, kThreads, smem, s>>>(static_cast<T*>(a.re), static_cast<T*>(a.im),
+                                                  static_cast<const TcDesc<K>*>(a.desc), a.err);
   return cudaGetLastError();
 }
 
 cudaError_t launch_pass_tc(const LaunchArgs& a, cudaStream_t s) {
-  if (a.arith != AR_DF64 || !a.err) return cudaErrorInvalidValue;
-  if (a.K == 3) return launch_tc_k<3>(a, s);
-  if (a.K == 4) return launch_tc_k<4>(a, s);
+  if (!a.err || (a.K != 3 && a.K != 4)) return cudaErrorInvalidValue;
+  if (a.arith == AR_DF64) return a.K == 3 ? launch_tc_k<3, df64>(a, s) : launch_tc_k<4, df64>(a, s);
+  if (a.arith == AR_FP32) return a.K == 3 ? launch_tc_k<3, float>(a, s) : launch_tc_k<4, float>(a, s);
   return cudaErrorInvalidValue;
 }
 
-template <int K>
+template <int K, typename T>
 static int tc_occ() {
-  constexpr size_t smem = tc_smem_bytes<K>();
-  cudaFuncSetAttribute(k_pass_tc<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  constexpr size_t smem = tc_smem_bytes<K, T>();
+  cudaFuncSetAttribute(k_pass_tc<K, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pass_tc<K>, kThreads, smem) != cudaSuccess) return 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pass_tc<K, T>, kThreads, smem) != cudaSuccess) return 1;
   // TMEM: 512 columns per SM shared by the resident blocks
-  const int tmem_cap = 512 / (int)TcShape<K>::TMEM_COLS;
+  const int tmem_cap = 512 / (int)TcShape<K, T>::TMEM_COLS;
   nb = nb < tmem_cap ? nb : tmem_cap;
   return nb > 0 ? nb : 1;
 }
 
-int tc_blocks_per_sm(int K) { return K == 3 ? tc_occ<3>() : tc_occ<4>(); }
+int tc_blocks_per_sm(int K, int arith) {
+  if (arith == AR_FP32) return K == 3 ? tc_occ<3, float>() : tc_occ<4, float>();
+  return K == 3 ? tc_occ<3, df64>() : tc_occ<4, df64>();
+}
 
 }  // namespace dmg

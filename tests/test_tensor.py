@@ -93,3 +93,26 @@ def test_chained_runs_and_small_states(engine, oracle):
     r1 = oracle.dm_sim(n, circ)
     ref = oracle.dm_sim(n, circ + circ)
     assert maxerr((re, im), ref) <= 1e-10 * max(1.0, np.abs(r1[0]).max())
+
+
+def test_complex64_tensor_passes(engine):
+    """complex64 (FP32 state, 3 BF16 slices per operand): the tensor-core
+    passes are as accurate as the FP32-pipe ones against an FP64 run."""
+    n = 10
+    circ = W.u3_cx_ccx(n, 300, seed=3)
+    errs = {}
+    with engine.Simulation(n, mode="plain") as ref:
+        ref.extend(circ)
+        ref.upload()
+        ref.run()
+        for tensor in (0, "all"):
+            with engine.Simulation(n, mode="fused", precision="c64", tensor=tensor) as s:
+                s.extend(circ)
+                s.upload()
+                s.set_option(engine.OPT_RECORD, 1)
+                s.run()
+                ran_tc = s.pass_records()[:, 8].sum() > 0
+                errs[tensor] = (s.compare(ref)["max_abs_err"], ran_tc)
+    assert errs["all"][1] and not errs[0][1]
+    assert errs["all"][0] <= 1e-5 and errs[0][0] <= 1e-5, errs
+    assert errs["all"][0] <= 4 * errs[0][0] + 1e-7, errs
