@@ -230,15 +230,8 @@ std::vector<PassSpec> make_plan(dmsim_sim* s, const std::vector<Basic>& basics) 
 
 void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_basic, int arith);
 
-// A double-float or complex64 pass of 3 or 4 qubits with at least kTcMinRowNnz nonzeros
-// per row of U runs on the tensor cores: their cost does not depend on the
-// density, the FP32-pipe kernel's grows with it.
-constexpr int kTcMinRowNnz = 3;
 bool use_tensor(const dmsim_sim* s, const PassSpec& p, int arith) {
-  if (!s->tensor || (arith != AR_DF64 && arith != AR_FP32) || !tc_eligible(p, (int)s->n)) return false;
-  if (s->tensor == 2) return true;    // every eligible pass (measurements)
-  if (p.tc >= 0) return p.tc != 0;    // the learned planner's choice
-  return p.nnz >= kTcMinRowNnz * (1 << p.K);
+  return tc_choose(p, (int)s->n, s->tensor, arith);
 }
 
 void upload(dmsim_sim* s) {
@@ -1039,6 +1032,7 @@ int dmsim_plan_inspect(uint32_t n_qubits, const int32_t* ops, const uint32_t* qu
         o[2] = p.nbasic;
         o[3] = p.nnz;
         for (int k = 0; k < p.K; k++) o[4 + k] = p.q[k];
+        o[10] = (mode == 1 && tc_choose(p, (int)n_qubits, 1, AR_DF64)) ? 1 : 0;
         o[8] = p.ket_only ? 1 : 0;
         o[9] = p.transpose ? 1 : 0;
         if (p.transpose) continue;

@@ -588,6 +588,13 @@ bool tc_eligible(const PassSpec& p, int n) {
   return 2 * n - 2 * p.K >= 7 - p.K;
 }
 
+bool tc_choose(const PassSpec& p, int n, int tensor_opt, int arith) {
+  if (!tensor_opt || (arith != 2 && arith != 1) || !tc_eligible(p, n)) return false;  // double-float or FP32 state
+  if (tensor_opt == 2) return true;  // every eligible pass (measurements)
+  if (p.tc >= 0) return p.tc != 0;   // the learned planner's choice
+  return p.nnz >= kTcMinRowNnz * (1 << p.K);
+}
+
 size_t tc_desc_bytes(int K) { return K == 3 ? sizeof(TcDesc<3>) : sizeof(TcDesc<4>); }
 
 uint64_t build_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries,

@@ -68,6 +68,12 @@ uint64_t build_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64
 // whether a pass can run on the tensor cores, the size of its descriptor
 // (TcDesc<K>) and the descriptor itself.
 bool tc_eligible(const PassSpec& p, int n);
+// Whether an eligible pass runs there: option 0 never, 2 always, 1 the
+// learned planner's per-pass choice (PassSpec::tc) or, without one, at least
+// kTcMinRowNnz nonzeros per row of U (the tensor cores' cost does not depend
+// on the density, the FP32-pipe kernel's grows with it).
+constexpr int kTcMinRowNnz = 3;
+bool tc_choose(const PassSpec& p, int n, int tensor_opt, int arith);
 size_t tc_desc_bytes(int K);
 uint64_t build_tc_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries);
 

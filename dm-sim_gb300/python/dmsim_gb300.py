@@ -373,7 +373,8 @@ def plan_inspect(n, circuit, mode="fused", max_k=4, planner="greedy"):
         K = int(r[0])
         D = 1 << K
         rec = {"K": K, "cls": CLASS_NAMES[int(r[1])], "nbasic": int(r[2]), "nnz": int(r[3]),
-               "qubits": [int(x) for x in r[4:4 + K]], "ket_only": bool(r[8]), "transpose": bool(r[9])}
+               "qubits": [int(x) for x in r[4:4 + K]], "ket_only": bool(r[8]), "transpose": bool(r[9]),
+               "tensor": bool(r[10])}
         if rec["transpose"]:
             rec["cls"] = "TRANSPOSE"
         elif rec["cls"] == "RLIN":

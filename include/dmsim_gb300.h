@@ -159,7 +159,8 @@ int dmsim_free_host(void* p);
  * dmsim_upload would and return, per pass, DMSIM_PASS_REC doubles:
  * [0..7] {K, class, n_basic, nnz, q0, q1, q2, q3}, [8] ket-only flag,
  * [9] transpose flag (the reference-order adjoint stage, no operator),
- * [16..527] the ket operator U and [528..1039] the bra operator V (16x16
+ * [10] tensor-core flag (a fused double-float run with DMSIM_OPT_TENSOR = 1
+ * would run the pass on the tensor cores), [16..527] the ket operator U and [528..1039] the bra operator V (16x16
  * complex, re/im interleaved, row stride 2^K; for the real-linear class the
  * 4x4 real ket and bra maps).  ops[i], qubits[5*i..], params[3*i..] = theta,
  * phi, lambda; mats[32*i..] holds C1/C2 matrices (may be NULL when there are
