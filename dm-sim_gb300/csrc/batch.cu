@@ -177,6 +177,7 @@ template <typename T>
 static int blocks_t() {
   const size_t smem = batch_smem_bytes();
   cudaFuncSetAttribute(k_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(k_batch<T>, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<T>, kThreads, smem) != cudaSuccess) return 1;
   return nb > 0 ? nb : 1;
@@ -188,6 +189,9 @@ template <typename T>
 static cudaError_t launch_t(const BatchLaunch& a, cudaStream_t s) {
   const size_t smem = batch_smem_bytes();
   cudaError_t e = cudaFuncSetAttribute(k_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_batch<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
   // all-zero bytes are 0 in both FP64 and double-float
   e = cudaMemsetAsync(a.re, 0, a.total_entries * sizeof(double), s);

@@ -61,14 +61,27 @@ __global__ void __launch_bounds__(kThreads) k_pass(T* __restrict__ re, T* __rest
 }
 
 // ---------------------------------------------------------------- launchers
+// Dynamic shared memory for the largest tile, and the largest shared-memory
+// carveout so that the resident-block count the occupancy query reports is
+// the one the launches get.
+template <typename T, int K, int CLS>
+static cudaError_t configure_pass() {
+  constexpr int D = 1 << K;
+  cudaError_t e = cudaFuncSetAttribute(k_pass<T, K, CLS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)pass_smem_bytes<T, K, CLS>(kThreads * D));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_pass<T, K, CLS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+  return e;
+}
+
 template <typename T, int K, int CLS>
 static cudaError_t launch_one(const LaunchArgs& a, cudaStream_t s) {
   constexpr int D = 1 << K;
   const size_t smem = pass_smem_bytes<T, K, CLS>(a.tile_entries);
   static int configured = 0;  // per instance; attribute set once per process
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_pass<T, K, CLS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)pass_smem_bytes<T, K, CLS>(kThreads * D));
+    cudaError_t e = configure_pass<T, K, CLS>();
     if (e != cudaSuccess) return e;
     configured = 1;
   }
@@ -118,7 +131,7 @@ static int occ_one() {
   constexpr int D = 1 << K;
   int nb = 0;
   const size_t smem = pass_smem_bytes<T, K, CLS>(kThreads * D);
-  cudaFuncSetAttribute(k_pass<T, K, CLS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (configure_pass<T, K, CLS>() != cudaSuccess) return 1;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pass<T, K, CLS>, kThreads, smem) != cudaSuccess) return 1;
   return nb > 0 ? nb : 1;
 }

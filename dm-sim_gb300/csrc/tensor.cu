@@ -377,12 +377,24 @@ __global__ void __launch_bounds__(kThreads, 2) k_pass_tc(T* __restrict__ re, T* 
   if (tid < 32) tc::tmem_dealloc(tmem, SH::TMEM_COLS);
 }
 
+// Dynamic shared memory and the largest shared-memory carveout: without the
+// carveout preference the runtime may configure the SM for one 110 KB block.
+template <int K, typename T>
+static cudaError_t configure_tc() {
+  constexpr size_t smem = tc_smem_bytes<K, T>();
+  cudaError_t e = cudaFuncSetAttribute(k_pass_tc<K, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_pass_tc<K, T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+  return e;
+}
+
 template <int K, typename T>
 static cudaError_t launch_tc_k(const LaunchArgs& a, cudaStream_t s) {
   constexpr size_t smem = tc_smem_bytes<K, T>();
   static int configured = 0;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_pass_tc<K, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = configure_tc<K, T>();
     if (e != cudaSuccess) return e;
     configured = 1;
   }
@@ -401,7 +413,7 @@ cudaError_t launch_pass_tc(const LaunchArgs& a, cudaStream_t s) {
 template <int K, typename T>
 static int tc_occ() {
   constexpr size_t smem = tc_smem_bytes<K, T>();
-  cudaFuncSetAttribute(k_pass_tc<K, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (configure_tc<K, T>() != cudaSuccess) return 1;
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pass_tc<K, T>, kThreads, smem) != cudaSuccess) return 1;
   // TMEM: 512 columns per SM shared by the resident blocks

@@ -6,7 +6,7 @@ fitted on the GPU by the library's own forward/backward/Adam kernels
 (dmsim_cost_train), and the weights are written where the learned planner
 looks for them by default (dm-sim_gb300/model/cost_mlp.bin, or --out).
 
-    python dm-sim_gb300/train_cost_model.py [--sizes 10,12,14] [--out PATH]
+    python dm-sim_gb300/train_cost_model.py [--sizes 10,12,14,16] [--out PATH]
 """
 import argparse
 import json
@@ -24,7 +24,7 @@ import dmsim_gb300 as E  # noqa: E402
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--sizes", default="10,12,14")
+    ap.add_argument("--sizes", default="10,12,14,16")
     ap.add_argument("--circuits", type=int, default=2)
     ap.add_argument("--gates", type=int, default=60)
     ap.add_argument("--steps", type=int, default=4000)
@@ -35,8 +35,10 @@ def main():
     feats, ms = [], []
     t0 = time.time()
     for i, n in enumerate(int(x) for x in args.sizes.split(",")):
+        # 16 qubits (68.7 GB of FP64 state): one shorter circuit, the passes are ~16x slower
+        circuits, gates = (args.circuits, args.gates) if n <= 14 else (1, max(8, args.gates // 3))
         for arith in (E.AR_DF64, E.AR_FP64, E.AR_FP32):
-            f, m = E.cost_collect(n, n_circuits=args.circuits, gates=args.gates, seed=100 * args.seed + 10 * i + arith,
+            f, m = E.cost_collect(n, n_circuits=circuits, gates=gates, seed=100 * args.seed + 10 * i + arith,
                                   arith=arith)
             feats.append(f)
             ms.append(m)
