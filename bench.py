@@ -248,7 +248,8 @@ def extra_workload(args):
     elif args.workload == "c64_17":
         n = 17
         circ = W.u3_cx_ccx(n, 1000, seed=5)
-        s = E.Simulation(n, mode="fused", max_k=args.max_k, precision="c64", planner=args.planner)
+        tensor = "all" if args.tensor == "all" else int(args.tensor)
+        s = E.Simulation(n, mode="fused", max_k=args.max_k, precision="c64", planner=args.planner, tensor=tensor)
         s.extend(circ)
         s.upload()
         clocks.start()

@@ -394,6 +394,7 @@ void run(dmsim_sim* s) {
       else if (p.renorm) r.feat.cls = kRecRenorm;
       r.ms = pms;
       r.bytes = p.bytes;
+      r.grid = p.grid;
       s->records.push_back(r);
     }
   }
@@ -896,6 +897,7 @@ int dmsim_pass_records(dmsim_handle s, double* out, uint32_t cap, uint32_t* coun
         o[6] = r.ms;
         o[7] = r.bytes;
         o[8] = r.feat.tc;
+        o[9] = r.grid;
       }
   });
 }

@@ -29,6 +29,7 @@ struct PassRecord {
   PassFeatures feat;
   double ms;
   double bytes;
+  unsigned grid;
 };
 
 }  // namespace dmg

@@ -77,14 +77,14 @@ struct PassDesc {
   PassOp<K> op;
 };
 
-// ---- tensor-core passes (K = 3, 4; double-float state)
+// ---- tensor-core passes (K = 3, 4; double-float or complex64 state)
 // The ket step multiplies each tile column x (2^K complex entries, as 2R
 // reals [re; im]) by the real embedding W = [[Ur, -Ui], [Ui, Ur]] (R x R,
 // R = 2^(K+1)); the bra step does the same with V.  Both factors are split
-// into kTcSlices BF16 "slices" of 8 bits each on a per-row (W) or per-column
-// (x) power-of-two grid, so every slice product is an exact integer and the
-// FP32 tensor-core sums of each order i + j are exact; the orders are
-// recombined in double-float.  The W/V slices are computed on the host.
+// into BF16 "slices" of 8 bits each on a per-row (W) or per-column (x)
+// power-of-two grid, so every slice product is an exact multiple of one unit
+// per order i + j and the FP32 tensor-core sums of each order are exact; the
+// orders are added in double-float.  The W/V slices are computed on the host.
 constexpr int kTcSlices = 6;
 
 #if defined(__CUDACC__)
@@ -102,9 +102,11 @@ DMG_HD constexpr uint32_t tc_kmajor_offset(uint32_t row, uint32_t k, uint32_t sb
 template <int K>
 struct TcDesc {
   static constexpr int D = 1 << K, R = 2 * D;
-  PassHeader h;                               // tile geometry, g = 7 - K (128 columns per step)
-  int32_t rexp[2][R];                         // row n of W (0) / V (1) scaled by 2^rexp is sum_j t_j 256^-j
-  alignas(16) uint16_t sl[2][kTcSlices][R * R];  // slices t_j (BF16 bits), K-major core-matrix layout
+  PassHeader h;  // tile geometry, g = 7 - K (128 columns per step)
+  // slices of W (0) and V (1): row n of W = sum_j sl[0][j][n][.], slice j on
+  // the grid 2^(e_n - 7 - 8j) with |W[n][.]| < 2^e_n (BF16 bits at true
+  // scale, K-major core-matrix layout)
+  alignas(16) uint16_t sl[2][kTcSlices][R * R];
 };
 
 }  // namespace dmg

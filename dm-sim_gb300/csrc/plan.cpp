@@ -551,22 +551,18 @@ uint64_t build_tc_k(const PassSpec& p, int n, TcDesc<K>* d, PassFeatures* feat, 
       }
       double mx = 0;
       for (int k = 0; k < R; k++) mx = std::max(mx, std::fabs(w[k]));
-      int rexp = 0;
-      if (mx > 0) {
-        int e;
-        std::frexp(mx, &e);  // mx in [2^(e-1), 2^e): |w * 2^(7-e)| < 128
-        rexp = std::min(60, std::max(-60, 7 - e));
-      }
-      d->rexp[side][row] = rexp;
+      int e = 0;
+      if (mx > 0) std::frexp(mx, &e);  // mx in [2^(e-1), 2^e)
       for (int k = 0; k < R; k++) {
-        double v = std::ldexp(w[k], rexp);
+        double v = w[k];
         for (int j = 0; j < kTcSlices; j++) {
-          const double t = std::nearbyint(v);  // |t| <= 128: exact in BF16
+          const double unit = std::ldexp(1.0, e - 7 - 8 * j);
+          const double t = mx > 0 ? std::nearbyint(v / unit) * unit : 0.0;  // |t| <= 128 units: exact in BF16
           const float tf = (float)t;
           uint32_t bits;
           std::memcpy(&bits, &tf, 4);
           d->sl[side][j][tc_kmajor_offset(row, k, 16 * R) / 2] = (uint16_t)(bits >> 16);
-          v = (v - t) * 256.0;
+          v -= t;
         }
       }
     }

@@ -4,16 +4,19 @@
 //
 // A tile is 128 columns of one step: in the ket step column m = (b, f) holds
 // the 2^K entries rho[(., b, f)], in the bra step column m = (a, f) holds
-// rho[(a, ., f)].  Each column is split into kTcSlices BF16 slices on its own
-// power-of-two grid (x * 2^sc = sum_i s_i 256^-i, |s_i| <= 256); the host did
-// the same per row for the operator (W * 2^rexp = sum_j t_j 256^-j, |t_j| <=
-// 128).  One thread issues, per order o = 0..kTcSlices, the MMAs of every
-// slice pair i + j = o into the FP32 accumulator D_o (TMEM columns o*R ..):
-// each product is an integer below 2^15 and every D_o sum stays below 2^24,
-// so the tensor cores add exactly.  The threads then read the orders back and
-// recombine them in double-float.  Error per step (numpy emulation of this
-// arithmetic on random unitaries and columns): below 2^-46 of |W row|_2 |x|_2,
-// dominated by the 48-bit slicing of x and W.
+// rho[(a, ., f)].  Each column is split into BF16 slices on its own
+// power-of-two grid: with |x| < 2^e over the column, slice i holds the part
+// of x on the grid 2^(e - 7 - 8i), an integer multiple |s_i| <= 256 of that
+// unit (kept at its true scale, so a slice is exact in BF16); the host did the
+// same per row for the operator (|t_j| <= 128 units of 2^(e_row - 7 - 8j)).
+// One thread issues, per order o, the MMAs of every slice pair i + j = o into
+// the FP32 accumulator D_o (TMEM columns o*R ..): within D_o every product is
+// an integer multiple of one unit and the sum stays below 2^22.6 units, so
+// the tensor cores add exactly and D_o is the true partial sum.  The threads
+// then read the orders back and add them in double-float (FP32 for complex64).
+// Error per step (numpy emulation of this arithmetic on random unitaries and
+// columns): below 2^-46 of |W row|_2 |x|_2 for double-float, dominated by the
+// 48-bit slicing of x and W.
 //
 // Threads: 256.  Thread (warp w, lane l) owns column m = 32*(w & 3) + l (the
 // TMEM lane its warp may read) and half hf = w >> 2 of it: hf = 0 slices and
@@ -58,7 +61,6 @@ struct TcTables {
   uint64_t hioff[256];
   uint32_t ldmask[8], stmask[8];
   int lk[D], lb[D];
-  int rexp[2][R];
   float colmax[2][128];
   uint64_t bar;
   uint32_t slot;
@@ -71,44 +73,49 @@ constexpr size_t tc_smem_bytes() {
          sizeof(TcTables<K>);
 }
 
-// The slices of x = h + l (double-float) on the grid 2^-lsc: s[i] (integers,
-// |s| <= 256) with x * 2^lsc = sum_i s[i] 256^-i + (residual < 256^-(S-1)).
-// The low part cannot reach slices 0..2 (|l| <= 2^-24 |h| and |h * 2^lsc| <
-// 128), so it is sliced from slice 3 on and added there.
+// Rounding to the grid of slice i of a column whose largest |entry| has
+// biased FP32 exponent eb (|x| < 2^(eb-126)): (v + C_i) - C_i with
+// C_i = 1.5 * 2^(eb - 110 - 8i) rounds |v| < 2^22 units 2^(eb - 133 - 8i).
+__device__ __forceinline__ float slice_magic(int eb, int i) {
+  return __int_as_float(((eb + 17 - 8 * i) << 23) | 0x400000);
+}
+
+// The slices of x = h + l (double-float).  Slices 0..2 come from h alone
+// (exact); its remainder (below half a unit of slice 2) plus l, whose size is
+// at most that, is rounded once to FP32 -- an error of at most one unit of
+// slice 5 -- and gives slices 3..5.
 template <int S>
-__device__ __forceinline__ void slice_df(float h, float l, float sc, float sc24, float (&s)[S]) {
-  const float C = 12582912.f;  // 1.5 * 2^23: (v + C) - C rounds |v| < 2^22 to an integer
-  float v = __fmul_rn(h, sc);
+__device__ __forceinline__ void slice_df(float h, float l, const float (&C)[S], float (&s)[S]) {
+  float v = h;
 #pragma unroll
-  for (int i = 0; i < S; i++) {
-    const float t = __fsub_rn(__fadd_rn(v, C), C);
+  for (int i = 0; i < 3; i++) {
+    const float t = __fsub_rn(__fadd_rn(v, C[i]), C[i]);
     s[i] = t;
-    v = __fmul_rn(__fsub_rn(v, t), 256.f);
+    v = __fsub_rn(v, t);
   }
-  float u = __fmul_rn(l, sc24);
+  v = __fadd_rn(v, l);
 #pragma unroll
   for (int i = 3; i < S; i++) {
-    const float t = __fsub_rn(__fadd_rn(u, C), C);
-    s[i] = __fadd_rn(s[i], t);
-    u = __fmul_rn(__fsub_rn(u, t), 256.f);
+    const float t = __fsub_rn(__fadd_rn(v, C[i]), C[i]);
+    s[i] = t;
+    v = __fsub_rn(v, t);
   }
 }
 
-// The slices of an FP32 value on the grid 2^-lsc (|x * 2^lsc| < 128).
+// The slices of an FP32 value.
 template <int S>
-__device__ __forceinline__ void slice_f(float x, float sc, float (&s)[S]) {
-  const float C = 12582912.f;
-  float v = __fmul_rn(x, sc);
+__device__ __forceinline__ void slice_f(float x, const float (&C)[S], float (&s)[S]) {
+  float v = x;
 #pragma unroll
   for (int i = 0; i < S; i++) {
-    const float t = __fsub_rn(__fadd_rn(v, C), C);
+    const float t = __fsub_rn(__fadd_rn(v, C[i]), C[i]);
     s[i] = t;
-    v = __fmul_rn(__fsub_rn(v, t), 256.f);
+    v = __fsub_rn(v, t);
   }
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
-  const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);  // exact: |a|, |b| <= 256 are integers
+  const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);  // exact: at most 8 significant bits each
   return *reinterpret_cast<const uint32_t*>(&v);
 }
 
@@ -152,14 +159,13 @@ __device__ bool tc_step(T* __restrict__ sre, T* __restrict__ sim, unsigned char*
   tb.colmax[hf][m] = mx;
   __syncthreads();
   mx = fmaxf(tb.colmax[0][m], tb.colmax[1][m]);
-  // mx < 2^(eb-126): scale by 2^(133-eb) so that |x * sc| < 128.  Columns
-  // whose largest entry is below 2^-87 keep the scale 2^93 (their slices
-  // underflow towards 0; absolute error < 2^-87).
+  // mx < 2^(eb-126).  Columns whose largest entry is below 2^-87 keep the
+  // grid of 2^-87 (their slices underflow towards 0; absolute error < 2^-87).
   int eb = (__float_as_int(mx) >> 23) & 0xFF;
   eb = max(eb, 40);
-  const int lsc = 133 - eb;
-  const float sc = __int_as_float((lsc + 127) << 23);
-  const float sc24 = __int_as_float((lsc + 24 + 127) << 23);
+  float C[S];
+#pragma unroll
+  for (int i = 0; i < S; i++) C[i] = slice_magic(eb, i);
 
   // ---- slices -> the A operand (row m, K index hf*D + c), 16 bytes per 8 values
 #pragma unroll
@@ -169,11 +175,11 @@ __device__ bool tc_step(T* __restrict__ sre, T* __restrict__ sim, unsigned char*
     for (int c = 0; c < 8; c += 2) {
       float s0[S], s1[S];
       if constexpr (DF) {
-        slice_df<S>(xh[c8 + c], xl[c8 + c], sc, sc24, s0);
-        slice_df<S>(xh[c8 + c + 1], xl[c8 + c + 1], sc, sc24, s1);
+        slice_df<S>(xh[c8 + c], xl[c8 + c], C, s0);
+        slice_df<S>(xh[c8 + c + 1], xl[c8 + c + 1], C, s1);
       } else {
-        slice_f<S>(xh[c8 + c], sc, s0);
-        slice_f<S>(xh[c8 + c + 1], sc, s1);
+        slice_f<S>(xh[c8 + c], C, s0);
+        slice_f<S>(xh[c8 + c + 1], C, s1);
       }
 #pragma unroll
       for (int i = 0; i < S; i++) pk[i][c >> 1] = pack_bf16(s0[i], s1[i]);
@@ -222,17 +228,14 @@ __device__ bool tc_step(T* __restrict__ sre, T* __restrict__ sim, unsigned char*
     {
       float q[D];
       tmem_ld_row<D>(trow + 6 * R, q);
+      tmem_ld_row<D>(trow + 5 * R, lo);
       tc::tmem_wait_ld();
 #pragma unroll
-      for (int a = 0; a < D; a++) lo[a] = __fmul_rn(q[a], 0x1p-48f);
-      tmem_ld_row<D>(trow + 5 * R, q);
-      tc::tmem_wait_ld();
-#pragma unroll
-      for (int a = 0; a < D; a++) lo[a] = __fmaf_rn(q[a], 0x1p-40f, lo[a]);
+      for (int a = 0; a < D; a++) lo[a] = __fadd_rn(q[a], lo[a]);
       tmem_ld_row<D>(trow + 4 * R, q);
       tc::tmem_wait_ld();
 #pragma unroll
-      for (int a = 0; a < D; a++) lo[a] = __fmaf_rn(q[a], 0x1p-32f, lo[a]);
+      for (int a = 0; a < D; a++) lo[a] = __fadd_rn(lo[a], q[a]);
     }
     tmem_ld_row<D>(trow + 3 * R, p3);
     tmem_ld_row<D>(trow + 2 * R, p2);
@@ -242,14 +245,10 @@ __device__ bool tc_step(T* __restrict__ sre, T* __restrict__ sim, unsigned char*
 #pragma unroll
     for (int a = 0; a < D; a++) {
       // orders 0..3 error-free (their sum spans more than 24 bits), 4..6 in lo
-      const df64 s1 = two_sum(p0[a], __fmul_rn(p1[a], 0x1p-8f));
-      const df64 s2 = two_sum(s1.hi, __fmul_rn(p2[a], 0x1p-16f));
-      const df64 s3 = two_sum(s2.hi, __fmul_rn(p3[a], 0x1p-24f));
-      const df64 y = fast_two_sum(s3.hi, __fadd_rn(__fadd_rn(__fadd_rn(s1.lo, s2.lo), s3.lo), lo[a]));
-      // y * 2^-(lsc + rexp): exact power-of-two scaling
-      const int fe = min(254, max(0, 127 - lsc - tb.rexp[BRA ? 1 : 0][hf * D + a]));  // 0: y is negligible
-      const float f = __int_as_float(fe << 23);
-      arr[base + lc[a]] = df64(__fmul_rn(y.hi, f), __fmul_rn(y.lo, f));
+      const df64 s1 = two_sum(p0[a], p1[a]);
+      const df64 s2 = two_sum(s1.hi, p2[a]);
+      const df64 s3 = two_sum(s2.hi, p3[a]);
+      arr[base + lc[a]] = fast_two_sum(s3.hi, __fadd_rn(__fadd_rn(__fadd_rn(s1.lo, s2.lo), s3.lo), lo[a]));
     }
   } else {
     static_assert(S == 3, "the FP32 recombination is written for orders 0..3");
@@ -260,12 +259,7 @@ __device__ bool tc_step(T* __restrict__ sre, T* __restrict__ sim, unsigned char*
     tmem_ld_row<D>(trow, p0);
     tc::tmem_wait_ld();
 #pragma unroll
-    for (int a = 0; a < D; a++) {
-      float y = __fmaf_rn(p3[a], 0x1p-24f, __fmul_rn(p2[a], 0x1p-16f));
-      y = __fadd_rn(__fmaf_rn(p1[a], 0x1p-8f, y), p0[a]);
-      const int fe = min(254, max(0, 127 - lsc - tb.rexp[BRA ? 1 : 0][hf * D + a]));
-      arr[base + lc[a]] = __fmul_rn(y, __int_as_float(fe << 23));
-    }
+    for (int a = 0; a < D; a++) arr[base + lc[a]] = __fadd_rn(p0[a], __fadd_rn(p1[a], __fadd_rn(p2[a], p3[a])));
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -315,7 +309,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_pass_tc(T* __restrict__ re, T* 
     tb.lk[tid] = lk;
     tb.lb[tid] = lb;
   }
-  if (tid < 2 * SH::R) tb.rexp[tid / SH::R][tid % SH::R] = dp->rexp[tid / SH::R][tid % SH::R];
   if (tid < 32) {
     tc::tmem_alloc(&tb.slot, SH::TMEM_COLS);
     tc::tmem_relinquish();
@@ -410,15 +403,29 @@ cudaError_t launch_pass_tc(const LaunchArgs& a, cudaStream_t s) {
   return cudaErrorInvalidValue;
 }
 
+// Resident blocks per SM from the kernel's own resources: shared memory
+// (plus the 1 KB the driver reserves per block), registers, threads and the
+// 512 TMEM columns.  (The runtime occupancy query reported one block for
+// this kernel although two fit; the launch statistics confirm two.)
 template <int K, typename T>
 static int tc_occ() {
   constexpr size_t smem = tc_smem_bytes<K, T>();
   if (configure_tc<K, T>() != cudaSuccess) return 1;
-  int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pass_tc<K, T>, kThreads, smem) != cudaSuccess) return 1;
-  // TMEM: 512 columns per SM shared by the resident blocks
-  const int tmem_cap = 512 / (int)TcShape<K, T>::TMEM_COLS;
-  nb = nb < tmem_cap ? nb : tmem_cap;
+  cudaFuncAttributes fa;
+  int dev = 0, smem_sm = 0, regs_sm = 0, threads_sm = 0;
+  if (cudaFuncGetAttributes(&fa, k_pass_tc<K, T>) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev) != cudaSuccess)
+    return 1;
+  const int by_smem = smem_sm / (int)(smem + fa.sharedSizeBytes + 1024);
+  const int by_regs = regs_sm / (fa.numRegs * kThreads);
+  const int by_threads = threads_sm / kThreads;
+  const int by_tmem = 512 / (int)TcShape<K, T>::TMEM_COLS;
+  int nb = by_smem;
+  nb = nb < by_regs ? nb : by_regs;
+  nb = nb < by_threads ? nb : by_threads;
+  nb = nb < by_tmem ? nb : by_tmem;
   return nb > 0 ? nb : 1;
 }
 

@@ -125,10 +125,10 @@ int dmsim_upload_bytes(dmsim_handle h, uint64_t* bytes);
 int dmsim_last_timings(dmsim_handle h, double out[3]);
 /* Per-pass records of the last recorded run (DMSIM_OPT_RECORD): for each pass
  * DMSIM_PASS_RECORD doubles {K, class, nnz, max_lo_bit, min_hi_bit, n, ms,
- * bytes, tensor (1: ran on the tensor cores)}.  Passes
+ * bytes, tensor (1: ran on the tensor cores), blocks launched}.  Passes
  * that apply no gates have K = 0 and class 16 (FP64 <-> double-float
  * conversion), 17 (conjugate transpose) or 18 (complex64 renormalisation). */
-#define DMSIM_PASS_RECORD 9
+#define DMSIM_PASS_RECORD 10
 int dmsim_pass_records(dmsim_handle h, double* out, uint32_t cap, uint32_t* count);
 /* Compare rho with a pure state psi (2^n complex, FP64) on the device:
  * out[0] = fidelity <psi|rho|psi>, out[1] = trace, out[2] = max |rho - psi psi^+|,
