@@ -114,6 +114,18 @@ __device__ __forceinline__ void slice_f(float x, const float (&C)[S], float (&s)
   }
 }
 
+// Asynchronous global -> shared copies of one entry pair (Ampere-style
+// cp.async: 16 bytes through L2 only, 8 bytes through L1).
+template <int BYTES>
+__device__ __forceinline__ void cp_async_pair(void* smem_dst, const void* gmem_src) {
+  if constexpr (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_u32(smem_dst)), "l"(gmem_src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(tc::smem_u32(smem_dst)), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);  // exact: at most 8 significant bits each
   return *reinterpret_cast<const uint32_t*>(&v);
@@ -127,9 +139,12 @@ __device__ __forceinline__ void tmem_ld_row(uint32_t taddr, float (&v)[D]) {
 
 // One step (ket when !BRA) on the tile in shared memory.  Returns false (the
 // same on every thread) if the tensor core did not signal completion in time.
-template <int K, typename T, bool BRA>
+// `after_mma` runs on every thread once the step's MMAs have completed (the
+// slice buffers are free again): the bra step starts the next tile's loads
+// there.
+template <int K, typename T, bool BRA, typename F>
 __device__ bool tc_step(T* __restrict__ sre, T* __restrict__ sim, unsigned char* sA, const unsigned char* sB,
-                        TcTables<K>& tb, uint32_t tmem, int lf_g, uint32_t& phase) {
+                        TcTables<K>& tb, uint32_t tmem, int lf_g, uint32_t& phase, const F& after_mma) {
   using SH = TcShape<K, T>;
   constexpr int D = SH::D, R = SH::R, S = SH::S, G = SH::G;
   constexpr bool DF = std::is_same<T, df64>::value;
@@ -219,6 +234,7 @@ __device__ bool tc_step(T* __restrict__ sre, T* __restrict__ sim, unsigned char*
   phase ^= 1u;
   if (!__syncthreads_and(done)) return false;
   tc::fence_after_sync();
+  after_mma();
 
   // ---- recombine the orders of outputs n = hf*D + a (a < D)
   const uint32_t trow = tmem + ((uint32_t)(32 * (w & 3)) << 16) + hf * D;
@@ -334,34 +350,70 @@ __global__ void __launch_bounds__(kThreads, 2) k_pass_tc(T* __restrict__ re, T* 
   const int L = h.L, runlen = 1 << L;
   uint32_t phase = 0;
   bool ok = true;
-  for (uint64_t t = blockIdx.x; t < h.ntiles; t += gridDim.x) {
+  // Tile t is loaded directly; every later tile is copied asynchronously
+  // into the slice buffers while the previous tile's bra step recombines and
+  // its runs are stored, then moved into the tile buffer.  Each thread
+  // prefetches, stores and moves the same entry pairs, so those three need no
+  // barrier between them.
+  static_assert(2 * SH::TILE * sizeof(T) <= S * SH::A_BYTES, "the next tile must fit in the slice buffers");
+  T* nre = reinterpret_cast<T*>(sA);
+  T* nim = nre + SH::TILE;
+  constexpr int PAIRS = SH::TILE / 2 / kThreads;
+  uint64_t t = blockIdx.x;
+  if (t < h.ntiles) {
     const uint64_t base = tile_base(h, t);
-    // ---- load every run (the tensor cores multiply structural zeros too)
     for (int e2 = tid; e2 < (SH::TILE >> 1); e2 += blockDim.x) {
       const int e = e2 << 1;
       const int run = e >> L;
       const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
-      const T2 vr = ld2<T>(re + ga);
-      const T2 vi = ld2<T>(im + ga);
-      *reinterpret_cast<T2*>(sre + e) = vr;
-      *reinterpret_cast<T2*>(sim + e) = vi;
+      *reinterpret_cast<T2*>(sre + e) = ld2<T>(re + ga);
+      *reinterpret_cast<T2*>(sim + e) = ld2<T>(im + ga);
     }
+  }
+  for (; t < h.ntiles; t += gridDim.x) {
     __syncthreads();
-    if (!tc_step<K, T, false>(sre, sim, sA, sB, tb, tmem, lf_g, phase) ||
-        !tc_step<K, T, true>(sre, sim, sA, sB, tb, tmem, lf_g, phase)) {
+    const uint64_t base = tile_base(h, t);
+    const uint64_t tn = t + gridDim.x;
+    const bool has_next = tn < h.ntiles;
+    const uint64_t base_n = has_next ? tile_base(h, tn) : 0;
+    auto nothing = [] {};
+    auto prefetch = [&] {
+      if (!has_next) return;
+#pragma unroll
+      for (int k = 0; k < PAIRS; k++) {
+        const int e = (tid + k * kThreads) << 1;
+        const int run = e >> L;
+        const uint64_t ga = base_n + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
+        cp_async_pair<2 * sizeof(T)>(nre + e, re + ga);
+        cp_async_pair<2 * sizeof(T)>(nim + e, im + ga);
+      }
+      cp_async_commit();
+    };
+    if (!tc_step<K, T, false>(sre, sim, sA, sB, tb, tmem, lf_g, phase, nothing) ||
+        !tc_step<K, T, true>(sre, sim, sA, sB, tb, tmem, lf_g, phase, prefetch)) {
       ok = false;
+      if (has_next) cp_async_wait_all();  // no copy may still target shared memory
       break;
     }
-    // ---- store the runs the pass changes
-    for (int e2 = tid; e2 < (SH::TILE >> 1); e2 += blockDim.x) {
-      const int e = e2 << 1;
+    // ---- store the runs the pass changes, then move the next tile in
+#pragma unroll
+    for (int k = 0; k < PAIRS; k++) {
+      const int e = (tid + k * kThreads) << 1;
       const int run = e >> L;
       if (!((tb.stmask[run >> 5] >> (run & 31)) & 1)) continue;
       const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
       st2<T>(re + ga, *reinterpret_cast<const T2*>(sre + e));
       st2<T>(im + ga, *reinterpret_cast<const T2*>(sim + e));
     }
-    __syncthreads();
+    if (has_next) {
+      cp_async_wait_all();
+#pragma unroll
+      for (int k = 0; k < PAIRS; k++) {
+        const int e = (tid + k * kThreads) << 1;
+        *reinterpret_cast<T2*>(sre + e) = *reinterpret_cast<const T2*>(nre + e);
+        *reinterpret_cast<T2*>(sim + e) = *reinterpret_cast<const T2*>(nim + e);
+      }
+    }
   }
   if (!ok && tid == 0) atomicExch(err, 1);
   tc::fence_before_sync();
