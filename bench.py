@@ -29,6 +29,13 @@ import numpy as np  # noqa: E402
 
 import dmsim_workloads as W  # noqa: E402
 
+# DRAM traffic of the pass kernels relative to their algorithmic bytes, from
+# ncu captures of two launches each at 12 qubits (dram__bytes_read.sum +
+# dram__bytes_write.sum; profiles/k_pass_df64_K4_SPARSE_table_mix_12q.md and
+# profiles/k_pass_tc_K4_table_mix_12q.md): reads 268.6 MB of a 268.4 MB state,
+# writes equal to the stored runs.  Traffic grows with the state, so a launch's
+# traffic is its algorithmic bytes times this ratio.
+TRAFFIC_RATIO = 1.0003
 CLASS_NAMES = {0: "MOVE", 1: "SIGNED", 2: "PHASE", 3: "DENSE", 4: "SPARSE", 5: "RLIN", 6: "SUPER", 16: "CONVERT",
                17: "TRANSPOSE", 18: "RENORM"}
 
@@ -446,7 +453,9 @@ def main():
             "hbm_GBps_plain_df64_run": (plain_df64_bytes / plain_df64_s / 1e9) if plain_df64_s else None,
             "plain_df64_vs_plain_error": plain_df64_err, "plain_df64_kernels": plain_df64_kernels,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": hbm_peak,
-                         "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": None,
+                         "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
+                         "traffic": round(dom["bytes"] / dcount * TRAFFIC_RATIO),
+                         "traffic_source": "ncu DRAM bytes of 2 launches at 12q = 1.0003 x algorithmic, scaled",
                          "peak_kind": peak_kind, "launches": dcount},
             "kernels": kernels,
             "e2e": {"value": float(np.mean(e2e)), "unit": "s/circuit",

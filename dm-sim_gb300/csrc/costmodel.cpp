@@ -237,7 +237,7 @@ std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int 
   std::vector<int> owner, pass_of;
   std::vector<char> is_tc;
   std::vector<unsigned char> buf(std::max(desc_size(kMaxK), tc_desc_bytes(kMaxK)));
-  const bool tc_ok = tensor && (arith == 2 || arith == 1);  // double-float or FP32 state
+  const bool tc_ok = tensor && arith == 2;  // double-float state (complex64 tensor passes are opt-in)
   for (size_t c = 0; c < cands.size(); c++)
     for (size_t i = 0; i < cands[c].size(); i++) {
       const PassSpec& p = cands[c][i];

@@ -75,7 +75,7 @@ struct dmsim_sim {
   int fused_arith = 1;  // fused FP64 runs compute in double-float (1) or FP64 (0)
   int plain_arith = 0;  // plain FP64 runs compute in FP64 (0) or double-float (1)
   int renorm = 64;      // complex64: renormalise every renorm passes (0 = never)
-  int tensor = 0;       // double-float K = 3, 4 dense/sparse passes on the tensor cores
+  int tensor = 1;       // K = 3, 4 dense/sparse passes on the tensor cores (DMSIM_OPT_TENSOR)
   int arith = 0;        // arithmetic of the uploaded plan (kernels.h Arith)
   int64_t seed = -1;
 

@@ -52,7 +52,6 @@ struct TcShape {
   static constexpr uint32_t TMEM_COLS =
       ORDERS * R <= 32 ? 32 : (ORDERS * R <= 64 ? 64 : (ORDERS * R <= 128 ? 128 : 256));
   static_assert(ORDERS * R <= 256, "accumulators exceed the tensor-memory allocation");
-  static constexpr uint32_t IDESC = tc::idesc_bf16_f32(128, R);
 };
 
 template <int K>
@@ -209,25 +208,29 @@ __device__ bool tc_step(T* __restrict__ sre, T* __restrict__ sim, unsigned char*
   __syncthreads();
   tc::fence_after_sync();
 
-  // ---- one thread issues every slice-pair product, grouped by order
+  // ---- one thread issues the products.  The operator's slices W_0..W_{S-1}
+  // are consecutive R-row blocks of one K-major operand, so A_i against
+  // W_j0..W_{j0+nb-1} is one MMA of N = nb*R whose block j lands in the
+  // accumulator of order i + j when its destination starts at column i*R.
+  // Seven MMAs (per 16-wide K chunk) cover every pair with i + j < ORDERS:
+  // A_0 W_0 -> D_0 and A_1 W_* -> D_1.. overwrite; the rest accumulate.
   if (tid == 0) {
     const uint32_t a0 = tc::smem_u32(sA);
     const uint32_t b0 = tc::smem_u32(sB) + (BRA ? S * SH::B_BYTES : 0);
+    auto issue = [&](int i, int j0, int nb, bool overwrite) {
 #pragma unroll
-    for (int o = 0; o < SH::ORDERS; o++) {
-      uint32_t acc = 0;
-#pragma unroll
-      for (int i = (o < S ? 0 : o - S + 1); i <= o && i < S; i++) {
-        const int j = o - i;
-#pragma unroll
-        for (int kk = 0; kk < R / 16; kk++) {
-          const uint64_t ad = tc::smem_desc(a0 + i * SH::A_BYTES + kk * 256, tc::kLbo, SH::SBO);
-          const uint64_t bd = tc::smem_desc(b0 + j * SH::B_BYTES + kk * 256, tc::kLbo, SH::SBO);
-          tc::mma_bf16(tmem + o * R, ad, bd, SH::IDESC, acc);
-          acc = 1;
-        }
+      for (int kk = 0; kk < R / 16; kk++) {
+        const uint64_t ad = tc::smem_desc(a0 + i * SH::A_BYTES + kk * 256, tc::kLbo, SH::SBO);
+        const uint64_t bd = tc::smem_desc(b0 + j0 * SH::B_BYTES + kk * 256, tc::kLbo, SH::SBO);
+        tc::mma_bf16(tmem + (i + j0) * R, ad, bd, tc::idesc_bf16_f32(128, nb * R), (overwrite && kk == 0) ? 0u : 1u);
       }
-    }
+    };
+    constexpr int O = SH::ORDERS;
+    issue(0, 0, 1, true);                            // (0,0)
+    issue(1, 0, S < O - 1 ? S : O - 1, true);        // (1,0) .. (1,min(S,O-1)-1)
+    issue(0, 1, S - 1, false);                       // (0,1) .. (0,S-1)
+#pragma unroll
+    for (int i = 2; i < S; i++) issue(i, 0, S < O - i ? S : O - i, false);  // (i,0) .. (i,O-1-i)
     tc::mma_commit(&tb.bar);
   }
   const bool done = tc::mbar_wait_bounded(&tb.bar, phase, 1u << 24);
