@@ -29,7 +29,8 @@ void pass_features(const PassFeatures& f, float* x) {
   x[12] = (float)(f.min_hi_bit / nb);
   x[13] = (float)(nb / 34.0);                     // log2 of the entry count
   x[14] = f.arith == 1 ? 1.f : (f.arith == 2 ? 0.5f : 0.f);  // FP32 / double-float / FP64
-  x[15] = (float)((f.nnz / (double)D) * f.ld_frac * std::ldexp(1.0, (int)nb - 28));  // arithmetic volume
+  // arithmetic volume (real operators need half the multiply-adds)
+  x[15] = (float)((f.nnz / (double)D) * f.ld_frac * std::ldexp(1.0, (int)nb - 28) * (f.real && !f.tc ? 0.5 : 1.0));
   x[16] = f.tc ? 1.f : 0.f;                       // on the tensor cores (cost independent of the density)
 }
 

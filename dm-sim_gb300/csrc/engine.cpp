@@ -170,6 +170,7 @@ void enqueue_passes(dmsim_sim* s, bool timed) {
     a.grid = p.grid;
     a.tile_entries = p.tile_entries;
     a.tc = p.tc;
+    a.real = p.real;
     a.err = s->d_err;
     if (timed) DM_CUDA(cudaEventRecord(p.ev0, s->stream));
     DM_CUDA(launch_pass(a, s->stream));
@@ -293,6 +294,7 @@ void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_b
         pi.tc ? build_tc_desc(specs[i], (int)s->n, blob.data() + offs[i], &pi.feat, &ntiles, &tile)
               : build_desc(specs[i], (int)s->n, blob.data() + offs[i], &pi.feat, &ntiles, &tile);
     pi.feat.tc = pi.tc ? 1 : 0;
+    pi.real = !pi.tc && pi.feat.real;
     pi.K = specs[i].K;
     pi.cls = specs[i].cls;
     pi.desc_off = offs[i];

@@ -18,6 +18,7 @@ struct PassInfo {
   double bytes;         // algorithmic bytes moved (reads + writes)
   int nbasic;
   bool tc;              // runs on the tensor cores (tensor.cu)
+  bool real;            // real operator (kernels_real.cu for K <= 2)
   PassFeatures feat;
   cudaEvent_t ev0, ev1; // per-pass timing (record mode)
 };

@@ -17,6 +17,7 @@ struct LaunchArgs {
   int arith;           // Arith
   unsigned grid;       // blocks
   int tile_entries;    // G * 4^K
+  bool real;           // DENSE/SPARSE pass whose U and V are real (pass.h kPassRealOperator)
   bool tc;             // tensor-core pass (desc is a TcDesc<K>; double-float or FP32 state, K = 3, 4)
   int* err;            // device flag set to 1 when a bounded wait of a tensor pass runs out
 };
@@ -25,6 +26,8 @@ struct LaunchArgs {
 cudaError_t launch_pass(const LaunchArgs& a, cudaStream_t s);
 // Resident blocks per SM of the kernel instance for (K, cls, arithmetic).
 int pass_blocks_per_sm(int K, int cls, int arith);
+// Real-operator instances of the 1- and 2-qubit DENSE/SPARSE kernels (kernels_real.cu).
+cudaError_t launch_pass_real(const LaunchArgs& a, cudaStream_t s);
 // Tensor-core passes (tensor.cu): launch, and resident blocks per SM.
 cudaError_t launch_pass_tc(const LaunchArgs& a, cudaStream_t s);
 int tc_blocks_per_sm(int K, int arith);

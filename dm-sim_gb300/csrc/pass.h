@@ -15,6 +15,12 @@
 #pragma once
 #include <stdint.h>
 
+#if defined(__CUDACC__)
+#define DMG_HD __host__ __device__
+#else
+#define DMG_HD
+#endif
+
 namespace dmg {
 
 constexpr int kThreads = 256;  // threads per block of every pass kernel
@@ -33,6 +39,17 @@ enum PassClass : int32_t {
   CLS_COUNT = 7
 };
 
+// Kernel instances for DENSE / SPARSE passes whose U and V are real (the
+// imaginary parts vanish, e.g. H, RY and their products with permutations):
+// two real multiply-adds per complex term instead of four.  The host classes
+// stay CLS_DENSE / CLS_SPARSE; PassHeader::flags marks such passes.
+constexpr int kClsRealOffset = 16;
+constexpr int CLS_DENSE_REAL = kClsRealOffset + CLS_DENSE;
+constexpr int CLS_SPARSE_REAL = kClsRealOffset + CLS_SPARSE;
+DMG_HD constexpr int base_class(int c) { return c >= kClsRealOffset ? c - kClsRealOffset : c; }
+DMG_HD constexpr bool real_class(int c) { return c >= kClsRealOffset; }
+constexpr int32_t kPassRealOperator = 1;  // PassHeader::flags bit
+
 // Factor kinds of a monomial superoperator entry f[a][b].
 enum FactorKind : int8_t { FK_ONE = 0, FK_NEG = 1, FK_PI = 2, FK_NI = 3, FK_GEN = 4 };
 
@@ -41,7 +58,7 @@ struct PassHeader {
   int32_t L;         // low run bits
   int32_t mhi;       // number of target bits >= L
   int32_t g;         // log2 of groups per tile
-  int32_t pad;
+  int32_t flags;     // kPassRealOperator: U and V are real
   uint64_t ntiles;   // tiles in the state
   int32_t hipos[8];  // global positions of the high target bits, ascending
   int32_t lket[4];   // local bit position of ket target i (qubit q_i)
@@ -87,11 +104,6 @@ struct PassDesc {
 // orders are added in double-float.  The W/V slices are computed on the host.
 constexpr int kTcSlices = 6;
 
-#if defined(__CUDACC__)
-#define DMG_HD __host__ __device__
-#else
-#define DMG_HD
-#endif
 // Byte offset of element (row, k) of a K-major, unswizzled BF16 tensor-core
 // operand: 8-row x 16-byte core matrices (128 contiguous bytes), 128 bytes
 // apart along k, `sbo` bytes apart between 8-row groups.

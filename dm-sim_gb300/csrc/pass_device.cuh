@@ -152,9 +152,10 @@ __device__ __forceinline__ int pext_local(int loc, const int* lpos) {
 
 // Per-pass constant tables, staged in shared memory once per block (or once
 // per work-queue range).  Arrays a class does not use shrink to one element.
-template <typename T, int K, int CLS>
+template <typename T, int K, int CLS_>
 struct PassTables {
   static constexpr int D = 1 << K;
+  static constexpr int CLS = base_class(CLS_);
   static constexpr bool kMat = CLS == CLS_DENSE || CLS == CLS_SPARSE;
   uint64_t hioff[256];
   uint32_t ldmask[8], stmask[8];
@@ -176,9 +177,10 @@ constexpr size_t pass_smem_bytes(int tile_entries) {
 }
 
 // All threads of the block; the caller synchronises afterwards.
-template <typename T, int K, int CLS>
-__device__ void load_tables(const PassDesc<K>* __restrict__ dp, PassTables<T, K, CLS>& tb) {
+template <typename T, int K, int CLS_>
+__device__ void load_tables(const PassDesc<K>* __restrict__ dp, PassTables<T, K, CLS_>& tb) {
   constexpr int D = 1 << K;
+  constexpr int CLS = base_class(CLS_);
   const int tid = threadIdx.x;
   const PassHeader& h = dp->h;
   const int mhi = h.mhi;
@@ -214,7 +216,7 @@ __device__ void load_tables(const PassDesc<K>* __restrict__ dp, PassTables<T, K,
   }
   for (int i = tid; i < D * D; i += blockDim.x) {
     tb.fk[i] = dp->op.fk[i];
-    if (PassTables<T, K, CLS>::kMat) {
+    if (PassTables<T, K, CLS_>::kMat) {
       tb.ure[i] = coef<T>(dp->op.ure[i]);
       tb.uim[i] = coef<T>(dp->op.uim[i]);
       tb.vre[i] = coef<T>(dp->op.vre[i]);
@@ -291,9 +293,9 @@ __device__ __forceinline__ void regs_to_smem(const PassHeader& h, const PassTabl
   }
 }
 
-template <typename T, int K, int CLS>
+template <typename T, int K, int CLS_>
 __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHeader& h,
-                          const PassTables<T, K, CLS>& tb, uint64_t base, T* __restrict__ sre, T* __restrict__ sim);
+                          const PassTables<T, K, CLS_>& tb, uint64_t base, T* __restrict__ sre, T* __restrict__ sim);
 
 // One tile t of the pass on the state (re, im).  All threads of the block;
 // sre/sim hold G * 4^K entries each.  Ends synchronised.
@@ -323,10 +325,12 @@ __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeade
 
 // The transform and the store of one tile whose touched runs are in shared
 // memory (after a barrier).  Ends synchronised.
-template <typename T, int K, int CLS>
+template <typename T, int K, int CLS_>
 __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHeader& h,
-                          const PassTables<T, K, CLS>& tb, uint64_t base, T* __restrict__ sre, T* __restrict__ sim) {
+                          const PassTables<T, K, CLS_>& tb, uint64_t base, T* __restrict__ sre, T* __restrict__ sim) {
   constexpr int D = 1 << K;
+  constexpr int CLS = base_class(CLS_);
+  constexpr bool RE = real_class(CLS_);  // U and V real: two multiply-adds per term
   using T2 = typename Vec2<T>::type;
   const int tid = threadIdx.x;
   const int L = h.L, g = h.g;
@@ -403,11 +407,14 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
           Acc<T> ar, ai;
 #pragma unroll
           for (int c = 0; c < D; c++) {
-            const T ur = tb.ure[a * D + c], ui = tb.uim[a * D + c];
+            const T ur = tb.ure[a * D + c];
             ar.mad(ur, xr[c]);
-            ar.mad(-ui, xi[c]);
             ai.mad(ur, xi[c]);
-            ai.mad(ui, xr[c]);
+            if constexpr (!RE) {
+              const T ui = tb.uim[a * D + c];
+              ar.mad(-ui, xi[c]);
+              ai.mad(ui, xr[c]);
+            }
           }
           sre[cb + tb.lk[a]] = ar.get();
           sim[cb + tb.lk[a]] = ai.get();
@@ -419,12 +426,15 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
           for (int a = 0; a < D; a++) {
             if (j < tb.nnz[a]) {
               const int c = tb.col[a * D + j];
-              const T ur = tb.ure[a * D + c], ui = tb.uim[a * D + c];
+              const T ur = tb.ure[a * D + c];
               const T vr = sre[cb + tb.lk[c]], vi = sim[cb + tb.lk[c]];
               yr[a].mad(ur, vr);
-              yr[a].mad(-ui, vi);
               yi[a].mad(ur, vi);
-              yi[a].mad(ui, vr);
+              if constexpr (!RE) {
+                const T ui = tb.uim[a * D + c];
+                yr[a].mad(-ui, vi);
+                yi[a].mad(ui, vr);
+              }
             }
           }
         }
@@ -461,11 +471,14 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
           Acc<T> ar, ai;
 #pragma unroll
           for (int c = 0; c < D; c++) {
-            const T vr = tb.vre[b * D + c], vi = tb.vim[b * D + c];
+            const T vr = tb.vre[b * D + c];
             ar.mad(vr, xr[c]);
-            ar.mad(-vi, xi[c]);
             ai.mad(vr, xi[c]);
-            ai.mad(vi, xr[c]);
+            if constexpr (!RE) {
+              const T vi = tb.vim[b * D + c];
+              ar.mad(-vi, xi[c]);
+              ai.mad(vi, xr[c]);
+            }
           }
           sre[ca + tb.lb[b]] = ar.get();
           sim[ca + tb.lb[b]] = ai.get();
@@ -477,12 +490,15 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
           for (int b = 0; b < D; b++) {
             if (j < tb.nnzb[b]) {
               const int c = tb.colb[b * D + j];
-              const T mr = tb.vre[b * D + c], mi = tb.vim[b * D + c];
+              const T mr = tb.vre[b * D + c];
               const T vr = sre[ca + tb.lb[c]], vi = sim[ca + tb.lb[c]];
               yr[b].mad(mr, vr);
-              yr[b].mad(-mi, vi);
               yi[b].mad(mr, vi);
-              yi[b].mad(mi, vr);
+              if constexpr (!RE) {
+                const T mi = tb.vim[b * D + c];
+                yr[b].mad(-mi, vi);
+                yi[b].mad(mi, vr);
+              }
             }
           }
         }

@@ -386,12 +386,15 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
   h.ntiles = 1ull << (nb - L - h.mhi);
 
   // operator tables
+  bool real = p.cls == CLS_DENSE || p.cls == CLS_SPARSE;
   for (int i = 0; i < D * D; i++) {
     op.ure[i] = p.U[i].real();
     op.uim[i] = p.U[i].imag();
     op.vre[i] = p.V[i].real();
     op.vim[i] = p.V[i].imag();
+    real = real && op.uim[i] == 0.0 && op.vim[i] == 0.0;
   }
+  if (real) h.flags |= kPassRealOperator;
   std::memcpy(op.rlin, p.rl, sizeof op.rlin);
   std::memcpy(op.rlinb, p.rlb, sizeof op.rlinb);
   if (p.cls == CLS_SUPER && K <= 2) {
@@ -503,6 +506,7 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
     feat->K = K;
     feat->cls = p.cls;
     feat->nnz = p.nnz;
+    feat->real = real ? 1 : 0;
     feat->n = n;
     int lo = -1, hmin = nb;
     for (int x : P) {

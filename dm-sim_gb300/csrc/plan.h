@@ -36,6 +36,7 @@ struct PassFeatures {
   int n;
   double ld_frac, st_frac;  // fraction of the state read / written
   int tc;           // 1: the pass runs on the tensor cores
+  int real;         // 1: U and V are real (half the multiply-adds on the FP32 pipe)
 };
 
 // Fusion planners.  Both keep program order on every qubit and only reorder
