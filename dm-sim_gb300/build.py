@@ -70,7 +70,7 @@ def build(force=False, verbose=False):
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             list(ex.map(run, jobs))
     if force or jobs or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        run([nv] + ARCH + ["-shared", "-o", LIB] + objs)
+        run([nv] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"])
     return LIB
 
 

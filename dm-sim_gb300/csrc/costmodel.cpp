@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <random>
+#include <thread>
 
 namespace dmg {
 
@@ -223,50 +224,70 @@ bool cost_model_predict(const CostModel& m, const std::vector<float>& X, std::ve
 std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int maxk, int arith, bool tensor,
                                    const CostModel& m, double* predicted_ms, std::string& err) {
   // candidate plans: the unfused plan, and greedy plans of every width up to
-  // maxk under row-density caps
-  std::vector<std::vector<PassSpec>> cands;
-  cands.push_back(plan_plain(basics));
+  // maxk under row-density caps.  Each candidate is planned and featurised on
+  // its own host thread (features of every pass and of its tensor-core
+  // variant where there is one), then one batched GPU inference scores all.
+  struct Cand {
+    int k, cap;
+    std::vector<PassSpec> plan;
+    std::vector<float> X;
+    std::vector<int> pass_of;
+    std::vector<char> is_tc;
+  };
+  std::vector<Cand> cands;
+  cands.push_back({1, kMaxD, {}, {}, {}, {}});
   const int caps[] = {kMaxD, 8, 4, 2};
   for (int k = 2; k <= maxk; k++)
     for (int cap : caps) {
       if (cap >= (1 << k) && cap != kMaxD) continue;  // no effect at this width
-      cands.push_back(plan_greedy(basics, k, cap));
+      cands.push_back({k, cap, {}, {}, {}, {}});
     }
-  // features of every pass of every candidate (and of its tensor-core
-  // variant where there is one), one batched inference
-  std::vector<float> X;
-  std::vector<int> owner, pass_of;
-  std::vector<char> is_tc;
-  std::vector<unsigned char> buf(std::max(desc_size(kMaxK), tc_desc_bytes(kMaxK)));
   const bool tc_ok = tensor && arith == 2;  // double-float state (complex64 tensor passes are opt-in)
-  for (size_t c = 0; c < cands.size(); c++)
-    for (size_t i = 0; i < cands[c].size(); i++) {
-      const PassSpec& p = cands[c][i];
+  auto work = [&](Cand& c) {
+    c.plan = c.k == 1 ? plan_plain(basics) : plan_greedy(basics, c.k, c.cap);
+    std::vector<unsigned char> buf(std::max(desc_size(kMaxK), tc_desc_bytes(kMaxK)));
+    for (size_t i = 0; i < c.plan.size(); i++) {
+      const PassSpec& p = c.plan[i];
       if (p.transpose) continue;
       for (int v = 0; v < 2; v++) {
         if (v == 1 && !(tc_ok && tc_eligible(p, n))) break;
         PassFeatures f;
         std::memset(&f, 0, sizeof f);
         if (v == 0) build_desc(p, n, buf.data(), &f, nullptr, nullptr);
-        else build_tc_desc(p, n, buf.data(), &f, nullptr, nullptr);
+        else build_tc_desc(p, n, buf.data(), &f, nullptr, nullptr, false);
         f.arith = arith;
         f.tc = v;
         float x[kMlpIn];
         pass_features(f, x);
-        X.insert(X.end(), x, x + kMlpIn);
-        owner.push_back((int)c);
-        pass_of.push_back((int)i);
-        is_tc.push_back((char)v);
+        c.X.insert(c.X.end(), x, x + kMlpIn);
+        c.pass_of.push_back((int)i);
+        c.is_tc.push_back((char)v);
       }
     }
+  };
+  {
+    std::vector<std::thread> threads;
+    for (size_t c = 1; c < cands.size(); c++) threads.emplace_back(work, std::ref(cands[c]));
+    work(cands[0]);
+    for (std::thread& t : threads) t.join();
+  }
+  std::vector<float> X;
+  std::vector<int> owner, pass_of;
+  std::vector<char> is_tc;
+  for (size_t c = 0; c < cands.size(); c++) {
+    X.insert(X.end(), cands[c].X.begin(), cands[c].X.end());
+    pass_of.insert(pass_of.end(), cands[c].pass_of.begin(), cands[c].pass_of.end());
+    is_tc.insert(is_tc.end(), cands[c].is_tc.begin(), cands[c].is_tc.end());
+    owner.insert(owner.end(), cands[c].pass_of.size(), (int)c);
+  }
   std::vector<float> ms;
   if (!cost_model_predict(m, X, ms, err)) return {};
   // per pass: the cheaper variant
   std::vector<std::vector<float>> best_ms(cands.size());
   std::vector<std::vector<char>> best_tc(cands.size());
   for (size_t c = 0; c < cands.size(); c++) {
-    best_ms[c].assign(cands[c].size(), -1.f);
-    best_tc[c].assign(cands[c].size(), 0);
+    best_ms[c].assign(cands[c].plan.size(), -1.f);
+    best_tc[c].assign(cands[c].plan.size(), 0);
   }
   for (size_t r = 0; r < ms.size(); r++) {
     float& b = best_ms[owner[r]][pass_of[r]];
@@ -281,7 +302,7 @@ std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int 
       if (v > 0) tot[c] += v;
   const size_t best = (size_t)(std::min_element(tot.begin(), tot.end()) - tot.begin());
   if (predicted_ms) *predicted_ms = tot[best];
-  std::vector<PassSpec> plan = cands[best];
+  std::vector<PassSpec> plan = std::move(cands[best].plan);
   for (size_t i = 0; i < plan.size(); i++) plan[i].tc = tc_ok ? best_tc[best][i] : -1;
   return plan;
 }

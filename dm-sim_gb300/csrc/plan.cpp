@@ -529,7 +529,7 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
 // real embeddings of U (ket) and V (bra).
 template <int K>
 uint64_t build_tc_k(const PassSpec& p, int n, TcDesc<K>* d, PassFeatures* feat, uint64_t* ntiles_out,
-                    int* tile_out) {
+                    int* tile_out, bool slices) {
   constexpr int D = 1 << K, R = 2 * D;
   std::unique_ptr<PassDesc<K>> geo(new PassDesc<K>);
   build_k<K>(p, n, geo.get(), feat, ntiles_out, tile_out, 7 - K);
@@ -543,7 +543,7 @@ uint64_t build_tc_k(const PassSpec& p, int n, TcDesc<K>* d, PassFeatures* feat, 
     nst += (h.stmask[r >> 5] >> (r & 31)) & 1;
   }
   if (feat) feat->ld_frac = 1.0;
-  for (int side = 0; side < 2; side++) {
+  for (int side = 0; side < 2 && slices; side++) {
     const cplx* M = side ? p.V : p.U;
     for (int row = 0; row < R; row++) {
       double w[R];
@@ -575,9 +575,10 @@ uint64_t build_tc_k(const PassSpec& p, int n, TcDesc<K>* d, PassFeatures* feat, 
   return (uint64_t)(nst + nruns) * runlen * h.ntiles;
 }
 
-uint64_t build_tc_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries) {
-  if (p.K == 3) return build_tc_k<3>(p, n, static_cast<TcDesc<3>*>(out), f, ntiles, tile_entries);
-  return build_tc_k<4>(p, n, static_cast<TcDesc<4>*>(out), f, ntiles, tile_entries);
+uint64_t build_tc_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries,
+                       bool slices) {
+  if (p.K == 3) return build_tc_k<3>(p, n, static_cast<TcDesc<3>*>(out), f, ntiles, tile_entries, slices);
+  return build_tc_k<4>(p, n, static_cast<TcDesc<4>*>(out), f, ntiles, tile_entries, slices);
 }
 
 bool tc_eligible(const PassSpec& p, int n) {

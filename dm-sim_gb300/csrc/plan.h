@@ -76,6 +76,8 @@ bool tc_eligible(const PassSpec& p, int n);
 constexpr int kTcMinRowNnz = 3;
 bool tc_choose(const PassSpec& p, int n, int tensor_opt, int arith);
 size_t tc_desc_bytes(int K);
-uint64_t build_tc_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries);
+// slices = false: geometry and features only (the planner's scoring).
+uint64_t build_tc_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries,
+                       bool slices = true);
 
 }  // namespace dmg
