@@ -361,6 +361,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         step_ms = float(t.item())
     bytes_per_run = fused.last_timings()["bytes"]
+    launches_per_run = int(fused.last_timings()["passes"])  # pass kernels + the two double-float conversions
 
     # ---- per-pass profile of one fused run (untimed): the dominant kernel
     kernels, dom, _ = class_profile(fused, "df64")
@@ -460,7 +461,7 @@ def main():
             "kernels": kernels,
             "e2e": {"value": float(np.mean(e2e)), "unit": "s/circuit",
                     "h2d_bytes_per_step": int(upload_bytes), "d2h_bytes_per_step": int(16 * N)},
-            "gpu_launches": int(npasses * args.steps),
+            "gpu_launches": launches_per_run * args.steps,
             "clocks": clk,
             "upload_s": upload_s,
             "wall_s_timed": wall,

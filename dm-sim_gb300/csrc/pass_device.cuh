@@ -295,7 +295,9 @@ __device__ __forceinline__ void regs_to_smem(const PassHeader& h, const PassTabl
 
 template <typename T, int K, int CLS_>
 __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHeader& h,
-                          const PassTables<T, K, CLS_>& tb, uint64_t base, T* __restrict__ sre, T* __restrict__ sim);
+                          const PassTables<T, K, CLS_>& tb, uint64_t base, T* __restrict__ sre, T* __restrict__ sim,
+                          int lf);
+__device__ __forceinline__ int free_offset(const PassHeader& h);
 
 // One tile t of the pass on the state (re, im).  All threads of the block;
 // sre/sim hold G * 4^K entries each.  Ends synchronised.
@@ -320,14 +322,24 @@ __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeade
     *reinterpret_cast<T2*>(sim + e) = vi;
   }
   __syncthreads();
-  tile_body<T, K, CLS>(re, im, h, tb, base, sre, sim);
+  tile_body<T, K, CLS>(re, im, h, tb, base, sre, sim, free_offset(h));
 }
 
 // The transform and the store of one tile whose touched runs are in shared
 // memory (after a barrier).  Ends synchronised.
+// Local offset of this thread's free group f = tid mod G (the same for every
+// tile of a pass).
+__device__ __forceinline__ int free_offset(const PassHeader& h) {
+  const int f = threadIdx.x & ((1 << h.g) - 1);
+  int lf = 0;
+  for (int j = 0; j < h.g; j++) lf |= ((f >> j) & 1) << h.freepos[j];
+  return lf;
+}
+
 template <typename T, int K, int CLS_>
 __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHeader& h,
-                          const PassTables<T, K, CLS_>& tb, uint64_t base, T* __restrict__ sre, T* __restrict__ sim) {
+                          const PassTables<T, K, CLS_>& tb, uint64_t base, T* __restrict__ sre, T* __restrict__ sim,
+                          int lf) {
   constexpr int D = 1 << K;
   constexpr int CLS = base_class(CLS_);
   constexpr bool RE = real_class(CLS_);  // U and V real: two multiply-adds per term
@@ -338,11 +350,6 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
   const int tile = G * D * D;
   const int runlen = 1 << L;
   const bool has_item = tid < G * D;
-  int lf = 0;
-  {
-    const int f = tid & (G - 1);
-    for (int j = 0; j < g; j++) lf |= ((f >> j) & 1) << h.freepos[j];
-  }
   const int r_item = tid >> g;  // b in the ket step, a in the bra step
 
   if constexpr (CLS == CLS_SUPER && K <= 2) {

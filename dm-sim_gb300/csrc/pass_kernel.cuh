@@ -32,6 +32,7 @@ __global__ void __launch_bounds__(kThreads) k_pass(T* __restrict__ re, T* __rest
       uint64_t t = blockIdx.x;
       if (t >= h.ntiles) return;
       TileRegs<T, P> x;
+      const int lf = free_offset(h);
       uint64_t base = tile_base(h, t);
       load_regs<T, K, CLS, P>(re, im, h, tb, base, x);
       for (; t < h.ntiles; t += gridDim.x) {
@@ -40,7 +41,7 @@ __global__ void __launch_bounds__(kThreads) k_pass(T* __restrict__ re, T* __rest
         const uint64_t tn = t + gridDim.x;
         const uint64_t base_n = tn < h.ntiles ? tile_base(h, tn) : 0;
         if (tn < h.ntiles) load_regs<T, K, CLS, P>(re, im, h, tb, base_n, x);
-        tile_body<T, K, CLS>(re, im, h, tb, base, sre, sim);
+        tile_body<T, K, CLS>(re, im, h, tb, base, sre, sim, lf);
         base = base_n;
       }
       return;
