@@ -6,7 +6,7 @@ One step = one run of the whole circuit on the device-resident rho (a CUDA
 graph replay of every pass).  ``value`` is seconds per circuit of the fused
 path (lower is better), device-timed with CUDA events on the engine's stream.
 Extra keys: the plain path's time and the speed-up, the fused-vs-plain error
-(the plain path judges every fused result), the roofline of the dominant pass
+(the plain path checks every fused result), the roofline of the dominant pass
 kernel, ``e2e`` through the C ABI with host buffers (the circuit and rho cross
 the host boundary every step), and a CPU baseline of the reference's CPU
 algorithm (the oracle port, all host cores) on a bounded prefix sample.

@@ -1,7 +1,9 @@
 // kernels.cu -- the superoperator pass kernels of the GB300 density-matrix engine.
 //
-// One kernel template covers every pass: precision T (double or float), width K
-// (1..4 qubits) and arithmetic class (pass.h).  A block owns one tile at a time
+// One kernel template (pass_kernel.cuh) covers every FP32-pipe / FP64 pass:
+// element type T (double, float, or double-float pairs), width K (1..4 qubits)
+// and arithmetic class (pass.h); the real-operator instances live in
+// kernels_real.cu and the tensor-core passes in tensor.cu.  A block owns one tile at a time
 // (grid-stride over tiles): it loads the tile's touched runs with 16-byte
 // vector loads into shared memory, transforms them, and stores them back.
 // Monomial classes (MOVE/SIGNED/PHASE) fuse the permutation and the per-entry
