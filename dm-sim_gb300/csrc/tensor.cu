@@ -287,8 +287,15 @@ __device__ bool tc_step(T* __restrict__ sre, T* __restrict__ sim, unsigned char*
 
 }  // namespace
 
+// Resident blocks the register budget is sized for: two double-float blocks
+// (TMEM: 2 x 256 columns), three complex64 blocks (3 x 128 columns), whose
+// per-tile work is light enough that the MMA round trips need more blocks to
+// overlap.
+template <typename T> struct TcMinBlocks { static constexpr int value = 2; };
+template <> struct TcMinBlocks<float> { static constexpr int value = 3; };
+
 template <int K, typename T>
-__global__ void __launch_bounds__(kThreads, 2) k_pass_tc(T* __restrict__ re, T* __restrict__ im,
+__global__ void __launch_bounds__(kThreads, TcMinBlocks<T>::value) k_pass_tc(T* __restrict__ re, T* __restrict__ im,
                                                          const TcDesc<K>* __restrict__ dp, int* __restrict__ err) {
   using SH = TcShape<K, T>;
   using T2 = typename Vec2<T>::type;
