@@ -242,7 +242,7 @@ std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int 
       if (cap >= (1 << k) && cap != kMaxD) continue;  // no effect at this width
       cands.push_back({k, cap, {}, {}, {}, {}});
     }
-  const bool tc_ok = tensor && arith == 2;  // double-float state (complex64 tensor passes are opt-in)
+  const bool tc_ok = tensor && (arith == 2 || arith == 1);  // double-float or complex64 state
   auto work = [&](Cand& c) {
     c.plan = c.k == 1 ? plan_plain(basics) : plan_greedy(basics, c.k, c.cap);
     std::vector<unsigned char> buf(std::max(desc_size(kMaxK), tc_desc_bytes(kMaxK)));

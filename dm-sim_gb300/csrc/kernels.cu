@@ -171,8 +171,9 @@ cudaError_t launch_conj_transpose(void* re, void* im, int n, bool fp32, unsigned
 
 // ---------------------------------------------------------------- renormalisation
 // complex64 mode: every R passes, trace(rho) is summed in FP64 and rho is made
-// Hermitian with unit trace, A <- (A + A^dagger) / (2 tr), in FP64 arithmetic
-// on the FP32 entries (tile pairs as in k_conj_transpose).
+// Hermitian with unit trace, A <- (A + A^dagger) / (2 tr), each entry in the
+// state's precision scaled by the FP64 trace (tile pairs as in
+// k_conj_transpose).
 template <typename T>
 __global__ void __launch_bounds__(256) k_trace(const T* __restrict__ re, int n, double* __restrict__ out) {
   const uint64_t dim = 1ull << n;
@@ -214,15 +215,14 @@ __global__ void __launch_bounds__(256) k_hermitise(T* __restrict__ re, T* __rest
     if (tx < ts)
       for (int ty = ty0; ty < ts; ty += 8) {
         const uint64_t ia = (I * ts + ty) * dim + J * ts + tx, ib = (J * ts + ty) * dim + I * ts + tx;
-        // new A[x][y] = (A[x][y] + conj(A[y][x])) / 2 / tr
-        const double ar = 0.5 * inv * ((double)a_re[ty][tx] + (double)b_re[tx][ty]);
-        const double ai = 0.5 * inv * ((double)a_im[ty][tx] - (double)b_im[tx][ty]);
-        const double br = 0.5 * inv * ((double)b_re[ty][tx] + (double)a_re[tx][ty]);
-        const double bi = 0.5 * inv * ((double)b_im[ty][tx] - (double)a_im[tx][ty]);
-        re[ia] = (T)ar;
-        im[ia] = (T)ai;
-        re[ib] = (T)br;
-        im[ib] = (T)bi;
+        // new A[x][y] = (A[x][y] + conj(A[y][x])) / 2 / tr, in the state's
+        // precision with the FP64 trace's scale (FP64 arithmetic on FP32
+        // entries would be bound by the f32 <-> f64 conversion rate)
+        const T h = (T)(0.5 * inv);
+        re[ia] = (a_re[ty][tx] + b_re[tx][ty]) * h;
+        im[ia] = (a_im[ty][tx] - b_im[tx][ty]) * h;
+        re[ib] = (b_re[ty][tx] + a_re[tx][ty]) * h;
+        im[ib] = (b_im[ty][tx] - a_im[tx][ty]) * h;
       }
     __syncthreads();
   }
