@@ -242,7 +242,10 @@ std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int 
       if (cap >= (1 << k) && cap != kMaxD) continue;  // no effect at this width
       cands.push_back({k, cap, {}, {}, {}, {}});
     }
-  const bool tc_ok = tensor && (arith == 2 || arith == 1);  // double-float or complex64 state
+  // double-float state only: at 17 qubits the model (trained up to 16) picked
+  // complex64 tensor passes that ran slower than the FP32 pipe (71.4 s against
+  // 62.5 s for the circuit); complex64 tensor passes stay opt-in (option 2)
+  const bool tc_ok = tensor && arith == 2;
   auto work = [&](Cand& c) {
     c.plan = c.k == 1 ? plan_plain(basics) : plan_greedy(basics, c.k, c.cap);
     std::vector<unsigned char> buf(std::max(desc_size(kMaxK), tc_desc_bytes(kMaxK)));

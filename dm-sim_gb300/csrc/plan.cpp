@@ -592,10 +592,8 @@ bool tc_eligible(const PassSpec& p, int n) {
 bool tc_choose(const PassSpec& p, int n, int tensor_opt, int arith) {
   if (!tensor_opt || (arith != 2 && arith != 1) || !tc_eligible(p, n)) return false;  // double-float or FP32 state
   if (tensor_opt == 2) return true;  // every eligible pass (measurements)
+  if (arith != 2) return false;      // complex64: opt-in only (option 2)
   if (p.tc >= 0) return p.tc != 0;   // the learned planner's choice
-  // complex64 without the planner's choice: the FP32 pipe (its tensor passes
-  // win only on dense operators)
-  if (arith != 2) return false;
   return p.nnz >= kTcMinRowNnz * (1 << p.K);
 }
 
