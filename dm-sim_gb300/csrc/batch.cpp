@@ -46,6 +46,8 @@ struct dmsim_batch {
   // tile shape: circuits of at most small_n qubits get log2(groups per tile)
   // reduced by g_shift (smaller tiles, more blocks on a small state)
   int small_n = 0, g_shift = 0;
+  unsigned wait_limit = 1u << 25;  // polls (128 ns naps) before a dependency wait gives up: ~4 s
+  int test_stall = 0;              // test hook: the last pass of circuit 0 waits for a tile that never comes
   std::string err;
 };
 
@@ -131,6 +133,7 @@ void build(dmsim_batch* b) {
       ranges.push_back(r);
       item += ntiles;
     }
+  if (b->test_stall && plans[0].size() >= 2) ranges[range_of[0].back()].dep_expected += 1;
   b->nranges = (int)ranges.size();
   b->nitems = item;
   b->bytes = bytes;
@@ -158,7 +161,7 @@ void build(dmsim_batch* b) {
   a.diag = b->d_diag;
   a.zz = b->d_zz;
   a.grid = b->grid;
-  a.spin_limit = 1u << 25;  // ~4 s of 128 ns naps before a wait gives up
+  a.spin_limit = b->wait_limit;
   a.df64_arith = b->mode == 1;  // fused batches compute in double-float, plain ones in FP64
   cudaGraph_t graph = nullptr;
   B_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -285,6 +288,11 @@ int dmsim_batch_set_option(dmsim_batch_handle b, int key, int64_t v) {
         b->maxk = (int)v;
         break;
       case DMSIM_OPT_PLANNER: b->planner = v != 0; break;
+      case DMSIM_BATCH_OPT_WAIT_LIMIT:
+        if (v < 1 || v > (int64_t)1 << 30) throw BErr{DMSIM_ERR_ARG, "wait limit must be 1..2^30 polls"};
+        b->wait_limit = (unsigned)v;
+        break;
+      case DMSIM_BATCH_OPT_TEST_STALL: b->test_stall = v != 0; break;
       default: throw BErr{DMSIM_ERR_ARG, "unsupported batch option"};
     }
   });

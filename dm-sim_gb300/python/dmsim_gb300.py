@@ -16,6 +16,7 @@ OK, ERR_ARG, ERR_STATE, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_UNSUPPORTED = range(
 (OPT_MODE, OPT_PRECISION, OPT_MAX_K, OPT_PLANNER, OPT_RECORD, OPT_SEED, OPT_GRAPH, OPT_VERBOSE, OPT_FUSED_ARITH,
  OPT_RENORM, OPT_PLAIN_ARITH, OPT_TENSOR) = range(1, 13)
 AR_FP64, AR_FP32, AR_DF64 = 0, 1, 2
+BATCH_OPT_WAIT_LIMIT, BATCH_OPT_TEST_STALL = 100, 101
 PASS_RECORD = 10  # doubles per pass record: K, class, nnz, max_lo_bit, min_hi_bit, n, ms, bytes, tensor, blocks
 
 OP_NAMES = ["U3", "U2", "U1", "CX", "ID", "X", "Y", "Z", "H", "S",
@@ -486,7 +487,7 @@ class Batch:
     from one captured CUDA graph.  Outputs per circuit: the diagonal and
     <Z_i Z_{i+1}>."""
 
-    def __init__(self, n_qubits_list, mode="fused", max_k=4, planner="greedy"):
+    def __init__(self, n_qubits_list, mode="fused", max_k=4, planner="greedy", wait_limit=None, test_stall=False):
         self.nq = [int(x) for x in n_qubits_list]
         self._h = ctypes.c_void_p()
         arr = (ctypes.c_uint32 * len(self.nq))(*self.nq)
@@ -496,6 +497,10 @@ class Batch:
         self._check(lib().dmsim_batch_set_option(self._h, OPT_MODE, 1 if mode == "fused" else 0))
         self._check(lib().dmsim_batch_set_option(self._h, OPT_MAX_K, int(max_k)))
         self._check(lib().dmsim_batch_set_option(self._h, OPT_PLANNER, 1 if planner == "learned" else 0))
+        if wait_limit is not None:
+            self._check(lib().dmsim_batch_set_option(self._h, BATCH_OPT_WAIT_LIMIT, int(wait_limit)))
+        if test_stall:
+            self._check(lib().dmsim_batch_set_option(self._h, BATCH_OPT_TEST_STALL, 1))
 
     def _check(self, st):
         if st != OK:

@@ -205,6 +205,13 @@ int dmsim_plan_predicted_ms(dmsim_handle h, double* ms);
  * gates, work items, algorithmic bytes, grid, tile-shape small_n, g_shift}.  No reference counterpart: the
  * reference runs circuits one Simulation at a time. */
 typedef struct dmsim_batch* dmsim_batch_handle;
+/* Batch-only options: the polls (128 ns naps) after which a work-queue
+ * dependency wait gives up [2^25, ~4 s] -- the kernel then sets an error flag,
+ * skips the item and finishes, and dmsim_batch_run returns
+ * DMSIM_ERR_TIMEOUT -- and a test hook that makes the last pass of circuit 0
+ * wait for one tile more than its predecessor has, so that its waits run
+ * out (failure detection without a GPU fault). */
+enum { DMSIM_BATCH_OPT_WAIT_LIMIT = 100, DMSIM_BATCH_OPT_TEST_STALL = 101 };
 int dmsim_batch_create(uint32_t n_circuits, const uint32_t* n_qubits, dmsim_batch_handle* out);
 int dmsim_batch_destroy(dmsim_batch_handle b);
 int dmsim_batch_set_option(dmsim_batch_handle b, int key, int64_t value);

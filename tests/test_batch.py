@@ -60,3 +60,29 @@ def test_hea_sweep_shape(engine, oracle):
             p = sr ** 2 + si ** 2
             assert np.abs(b.diag(c) - p).max() <= 1e-10
             assert np.abs(b.zz(c) - zz_from_diag(p, n)).max() <= 1e-9
+
+
+@pytest.mark.gpu
+def test_dependency_wait_runs_out_and_gpu_stays_usable(engine):
+    """Failure detection without a GPU fault: a wait whose count never
+    arrives gives up after the wait limit, the run reports a timeout, and the
+    next batch on the same device runs correctly."""
+    rng = np.random.default_rng(1)
+    sweep = [(4, W.hea(4, 3, rng)), (5, W.hea(5, 3, rng))]
+    with engine.Batch([n for n, _ in sweep], mode="plain", wait_limit=1 << 12, test_stall=True) as b:
+        for c, (n, circ) in enumerate(sweep):
+            b.extend(c, circ)
+        b.upload()
+        with pytest.raises(engine.DMSimError) as e:
+            b.run()
+        assert e.value.status == engine.ERR_TIMEOUT
+    with engine.Batch([n for n, _ in sweep], mode="plain") as b:
+        for c, (n, circ) in enumerate(sweep):
+            b.extend(c, circ)
+        b.upload()
+        b.run()
+        with engine.Simulation(4, mode="plain") as s:
+            s.extend(sweep[0][1])
+            s.upload()
+            s.run()
+            assert np.abs(s.get_diag() - b.diag(0)).max() <= 1e-12
