@@ -76,6 +76,7 @@ struct dmsim_sim {
   int plain_arith = 0;  // plain FP64 runs compute in FP64 (0) or double-float (1)
   int renorm = 64;      // complex64: renormalise every renorm passes (0 = never)
   int tensor = 1;       // K = 3, 4 dense/sparse passes on the tensor cores (DMSIM_OPT_TENSOR)
+  int direct1 = 1;      // 1-qubit passes on the register kernel (DMSIM_OPT_DIRECT1)
   int arith = 0;        // arithmetic of the uploaded plan (kernels.h Arith)
   int64_t seed = -1;
 
@@ -172,6 +173,9 @@ void enqueue_passes(dmsim_sim* s, bool timed) {
     a.tc = p.tc;
     a.real = p.real;
     a.err = s->d_err;
+    a.direct1 = p.direct1;
+    a.q0 = p.q0;
+    a.n = (int)s->n;
     if (timed) DM_CUDA(cudaEventRecord(p.ev0, s->stream));
     DM_CUDA(launch_pass(a, s->stream));
     if (timed) DM_CUDA(cudaEventRecord(p.ev1, s->stream));
@@ -305,6 +309,13 @@ void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_b
     const int bps = pi.tc ? tc_blocks_per_sm(pi.K, arith) : pass_blocks_per_sm(pi.K, pi.cls, arith);
     const uint64_t cap = (uint64_t)s->sms * (uint64_t)bps;
     pi.grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, cap));
+    // 1-qubit passes (n >= 2): one register-resident group of 4 entries per thread
+    pi.q0 = specs[i].q[0];
+    pi.direct1 = s->direct1 && !pi.tc && pi.K == 1 && s->n >= 2 && direct1_class(pi.cls);
+    if (pi.direct1) {
+      const uint64_t groups = 1ull << (2 * s->n - 2);
+      pi.grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((groups + 255) / 256, (uint64_t)s->sms * 8));
+    }
     s->passes.push_back(pi);
     // complex64: FP64 trace + Hermitian renormalisation every renorm passes and at the end
     if (s->fp32 && s->renorm > 0 && ((i + 1) % (size_t)s->renorm == 0 || i + 1 == specs.size())) {
@@ -554,6 +565,11 @@ int dmsim_set_option(dmsim_handle s, int key, int64_t v) {
         if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set the plain arithmetic before upload()"};
         s->plain_arith = v != 0;
         break;
+      case DMSIM_OPT_DIRECT1:
+        if (v != 0 && v != 1) throw DmError{DMSIM_ERR_ARG, "direct1 must be 0 or 1"};
+        if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set the 1-qubit kernel option before upload()"};
+        s->direct1 = (int)v;
+        break;
       case DMSIM_OPT_TENSOR:
         if (v < 0 || v > 2) throw DmError{DMSIM_ERR_ARG, "tensor must be 0, 1 or 2"};
         if (s->uploaded) throw DmError{DMSIM_ERR_STATE, "set the tensor-core option before upload()"};
@@ -585,6 +601,7 @@ int dmsim_get_option(dmsim_handle s, int key, int64_t* v) {
       case DMSIM_OPT_RENORM: *v = s->renorm; break;
       case DMSIM_OPT_PLAIN_ARITH: *v = s->plain_arith; break;
       case DMSIM_OPT_TENSOR: *v = s->tensor; break;
+      case DMSIM_OPT_DIRECT1: *v = s->direct1; break;
       default: throw DmError{DMSIM_ERR_ARG, "unknown option"};
     }
   });

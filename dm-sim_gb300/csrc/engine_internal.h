@@ -19,6 +19,8 @@ struct PassInfo {
   int nbasic;
   bool tc;              // runs on the tensor cores (tensor.cu)
   bool real;            // real operator (kernels_real.cu for K <= 2)
+  bool direct1;         // 1-qubit pass on the register kernel (kernels_k1.cu)
+  int q0;               // first target qubit
   PassFeatures feat;
   cudaEvent_t ev0, ev1; // per-pass timing (record mode)
 };

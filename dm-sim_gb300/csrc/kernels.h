@@ -20,12 +20,17 @@ struct LaunchArgs {
   bool real;           // DENSE/SPARSE pass whose U and V are real (pass.h kPassRealOperator)
   bool tc;             // tensor-core pass (desc is a TcDesc<K>; double-float or FP32 state, K = 3, 4)
   int* err;            // device flag set to 1 when a bounded wait of a tensor pass runs out
+  bool direct1;        // 1-qubit pass run by the register kernel (kernels_k1.cu)
+  int q0, n;           // its qubit and the state's qubit count
 };
 
 // Launch one pass on stream s.
 cudaError_t launch_pass(const LaunchArgs& a, cudaStream_t s);
 // Resident blocks per SM of the kernel instance for (K, cls, arithmetic).
 int pass_blocks_per_sm(int K, int cls, int arith);
+// 1-qubit MOVE / SIGNED / PHASE / DENSE passes without shared memory (kernels_k1.cu).
+bool direct1_class(int cls);
+cudaError_t launch_pass1(const LaunchArgs& a, cudaStream_t s);
 // Real-operator instances of the 1- and 2-qubit DENSE/SPARSE kernels (kernels_real.cu).
 cudaError_t launch_pass_real(const LaunchArgs& a, cudaStream_t s);
 // Tensor-core passes (tensor.cu): launch, and resident blocks per SM.

@@ -131,6 +131,25 @@ __device__ __forceinline__ void st2<df64>(df64* p, const df64x2& v) {
   __stcg(reinterpret_cast<float4*>(p), make_float4(v.x.hi, v.x.lo, v.y.hi, v.y.lo));
 }
 
+// Single-entry L2-coherent accesses.
+template <typename T>
+__device__ __forceinline__ T ld1(const T* p) {
+  return __ldcg(p);
+}
+template <>
+__device__ __forceinline__ df64 ld1<df64>(const df64* p) {
+  const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+  return df64(v.x, v.y);
+}
+template <typename T>
+__device__ __forceinline__ void st1(T* p, T v) {
+  __stcg(p, v);
+}
+template <>
+__device__ __forceinline__ void st1<df64>(df64* p, df64 v) {
+  __stcg(reinterpret_cast<float2*>(p), make_float2(v.hi, v.lo));
+}
+
 // Coefficients from the FP64 descriptor tables.
 template <typename T> __device__ __forceinline__ T coef(double x) { return (T)x; }
 template <> __device__ __forceinline__ df64 coef<df64>(double x) { return df64(x); }

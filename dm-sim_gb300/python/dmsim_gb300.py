@@ -14,7 +14,7 @@ LIB_PATH = os.path.normpath(os.path.join(_HERE, "..", "lib", "libdmsim_gb300.so"
 
 OK, ERR_ARG, ERR_STATE, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_UNSUPPORTED = range(7)
 (OPT_MODE, OPT_PRECISION, OPT_MAX_K, OPT_PLANNER, OPT_RECORD, OPT_SEED, OPT_GRAPH, OPT_VERBOSE, OPT_FUSED_ARITH,
- OPT_RENORM, OPT_PLAIN_ARITH, OPT_TENSOR) = range(1, 13)
+ OPT_RENORM, OPT_PLAIN_ARITH, OPT_TENSOR, OPT_DIRECT1) = range(1, 14)
 AR_FP64, AR_FP32, AR_DF64 = 0, 1, 2
 BATCH_OPT_WAIT_LIMIT, BATCH_OPT_TEST_STALL = 100, 101
 PASS_RECORD = 10  # doubles per pass record: K, class, nnz, max_lo_bit, min_hi_bit, n, ms, bytes, tensor, blocks
@@ -135,7 +135,7 @@ class Simulation:
     """
 
     def __init__(self, n_qubits, n_gpus=1, precision="fp64", mode="plain", max_k=4, planner="greedy",
-                 graph=True, fused_arith="df64", renorm=64, plain_arith="fp64", tensor=True):
+                 graph=True, fused_arith="df64", renorm=64, plain_arith="fp64", tensor=True, direct1=True):
         self._h = ctypes.c_void_p()
         self.n = int(n_qubits)
         st = lib().dmsim_create(self.n, int(n_gpus), ctypes.byref(self._h))
@@ -151,6 +151,7 @@ class Simulation:
             self.set_option(OPT_RENORM, int(renorm))
             self.set_option(OPT_PLAIN_ARITH, 1 if plain_arith == "df64" else 0)
             self.set_option(OPT_TENSOR, 2 if tensor == "all" else int(tensor))
+            self.set_option(OPT_DIRECT1, 1 if direct1 else 0)
         except Exception:
             self.close()
             raise
