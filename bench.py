@@ -245,7 +245,7 @@ def extra_workload(args):
             plain = E.Simulation(n, mode="plain")
             plain.extend(circ)
             plain.upload()
-            out["plain_kernels"], _, pms = class_profile(plain, "double")
+            out["plain_kernels"], _, pms = class_profile(plain, "df64")
             out["plain_s"] = pms / 1e3
             out["plain_GBps"] = plain.last_timings()["bytes"] / out["plain_s"] / 1e9
             out["speedup_fused_vs_plain"] = out["plain_s"] / out["fused_s"]
@@ -383,28 +383,27 @@ def main():
     err = None
     plain_bytes = None
     plain_passes = None
-    plain_df64_s = plain_df64_bytes = plain_df64_err = None
-    plain_kernels = plain_df64_kernels = None
+    plain_fp64_s = plain_fp64_bytes = plain_fp64_err = None
+    plain_kernels = plain_fp64_kernels = None
     if not args.no_plain:
-        plain = E.Simulation(n, mode="plain")
+        plain = E.Simulation(n, mode="plain")  # double-float passes, FP64 state
         plain.extend(circ)
         plain.upload()
-        plain_kernels, _, plain_ms = class_profile(plain, "double")  # per-pass events cost ~us per 3 ms pass
+        plain_kernels, _, plain_ms = class_profile(plain, "df64")  # per-pass events cost ~us per 1.3 ms pass
         plain_s = plain_ms / 1e3
         plain_bytes = plain.last_timings()["bytes"]
         plain_passes = plain.plan_stats()[0]
         fused.reset_dm()
         fused.run()
         err = fused.compare(plain)
-        # the same plain method with its passes in double-float (opt-in): the
-        # plain path's HBM rate when the FP64 pipe is out of the way
-        pdf = E.Simulation(n, mode="plain", plain_arith="df64")
+        # the same plain method with FP64 passes: bound by the FP64 pipe
+        pdf = E.Simulation(n, mode="plain", plain_arith="fp64")
         pdf.extend(circ)
         pdf.upload()
-        plain_df64_kernels, _, pdf_ms = class_profile(pdf, "df64")
-        plain_df64_s = pdf_ms / 1e3
-        plain_df64_bytes = pdf.last_timings()["bytes"]
-        plain_df64_err = pdf.compare(plain)
+        plain_fp64_kernels, _, pdf_ms = class_profile(pdf, "double")
+        plain_fp64_s = pdf_ms / 1e3
+        plain_fp64_bytes = pdf.last_timings()["bytes"]
+        plain_fp64_err = plain.compare(pdf)
         pdf.close()
         plain.close()
 
@@ -443,16 +442,17 @@ def main():
                        "planner": args.planner, "max_k": args.max_k, "tensor": args.tensor, "passes": npasses,
                        "basic_gates": nbasic,
                        "l2": "inputs larger than L2 (rho = %.1f GB)" % (16.0 * N / 1e9), "parallelism": "replicas"},
-            "state": "FP64 rho in and out; fused passes compute in double-float (FP32 hi+lo pairs)",
+            "state": "FP64 rho in and out; fused and plain passes compute in double-float (FP32 hi+lo pairs), "
+                     "dense 3/4-qubit fused passes on the tensor cores; plain_fp64_* = the plain path in FP64",
             "plain_s": plain_s, "plain_passes": plain_passes, "plain_kernels": plain_kernels,
             "greedy_s": greedy_s, "greedy_passes": greedy_passes,
             "speedup_fused_vs_plain": (plain_s / value) if plain_s else None,
             "fused_vs_plain_error": err,
             "hbm_GBps_fused_run": bytes_per_run / (step_ms * 1e-3) / 1e9,
             "hbm_GBps_plain_run": (plain_bytes / plain_s / 1e9) if plain_s else None,
-            "plain_df64_s": plain_df64_s,
-            "hbm_GBps_plain_df64_run": (plain_df64_bytes / plain_df64_s / 1e9) if plain_df64_s else None,
-            "plain_df64_vs_plain_error": plain_df64_err, "plain_df64_kernels": plain_df64_kernels,
+            "plain_fp64_s": plain_fp64_s,
+            "hbm_GBps_plain_fp64_run": (plain_fp64_bytes / plain_fp64_s / 1e9) if plain_fp64_s else None,
+            "plain_vs_plain_fp64_error": plain_fp64_err, "plain_fp64_kernels": plain_fp64_kernels,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": hbm_peak,
                          "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
                          "traffic": round(dom["bytes"] / dcount * TRAFFIC_RATIO),

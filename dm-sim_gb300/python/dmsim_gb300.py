@@ -135,7 +135,7 @@ class Simulation:
     """
 
     def __init__(self, n_qubits, n_gpus=1, precision="fp64", mode="plain", max_k=4, planner="greedy",
-                 graph=True, fused_arith="df64", renorm=64, plain_arith="fp64", tensor=True, direct1=True):
+                 graph=True, fused_arith="df64", renorm=64, plain_arith="df64", tensor=True, direct1=True):
         self._h = ctypes.c_void_p()
         self.n = int(n_qubits)
         st = lib().dmsim_create(self.n, int(n_gpus), ctypes.byref(self._h))

@@ -43,7 +43,8 @@ enum dmsim_option {
   DMSIM_OPT_VERBOSE = 8,    /* 1 = print the reference's per-run timing banner [0] */
   DMSIM_OPT_FUSED_ARITH = 9, /* fused FP64 runs: 1 = double-float passes on the FP32 pipe [1], 0 = FP64 passes */
   DMSIM_OPT_RENORM = 10,     /* complex64: FP64 trace + Hermitian renormalisation every R passes and at the end [64]; 0 = off */
-  DMSIM_OPT_PLAIN_ARITH = 11, /* plain FP64 runs: 0 = FP64 passes [0], 1 = double-float passes on the FP32 pipe */
+  DMSIM_OPT_PLAIN_ARITH = 11, /* plain FP64 runs (FP64 state at rest): 1 = double-float passes on the FP32 pipe [1],
+                                 0 = FP64 passes (bound by GB300's FP64 pipe) */
   DMSIM_OPT_TENSOR = 12,      /* 3- and 4-qubit dense/sparse passes on the tensor cores (BF16 slices, exact
                                  FP32 sums): 1 = where the learned planner (or, greedy, a density rule)
                                  picks them in double-float runs [1], 0 = FP32 pipe only, 2 = every eligible
