@@ -35,8 +35,8 @@ def main():
     feats, ms = [], []
     t0 = time.time()
     for i, n in enumerate(int(x) for x in args.sizes.split(",")):
-        # 16 qubits (68.7 GB of FP64 state): one shorter circuit, the passes are ~16x slower
-        circuits, gates = (args.circuits, args.gates) if n <= 14 else (1, max(8, args.gates // 3))
+        # 16 qubits (68.7 GB of FP64 state): shorter circuits, the passes are ~16x slower
+        circuits, gates = (args.circuits, args.gates) if n <= 14 else (2, max(8, args.gates // 2))
         for arith in (E.AR_DF64, E.AR_FP64, E.AR_FP32):
             f, m = E.cost_collect(n, n_circuits=circuits, gates=gates, seed=100 * args.seed + 10 * i + arith,
                                   arith=arith)
