@@ -35,6 +35,9 @@ void pass_features(const PassFeatures& f, float* x) {
   x[16] = f.tc ? 1.f : 0.f;                       // on the tensor cores (cost independent of the density)
 }
 
+// ln(4^n) of a pass from its features (x[13] = 2n / 34)
+double log_entries(const float* x) { return std::nearbyint(x[13] * 34.0) * std::log(2.0); }
+
 CostModel& global_cost_model() {
   static CostModel m;
   return m;
@@ -47,7 +50,7 @@ std::mutex& cost_model_mutex() {
 
 namespace {
 constexpr uint32_t kMagic = 0x434d4d44;  // "DMMC"
-constexpr uint32_t kVersion = 2;
+constexpr uint32_t kVersion = 3;  // 3: targets are log time per state entry
 }  // namespace
 
 bool cost_model_save(const CostModel& m, const std::string& path) {
@@ -66,10 +69,8 @@ bool cost_model_load(CostModel& m, const std::string& path) {
   if (!f) return false;
   uint32_t hdr[4];
   bool ok = fread(hdr, sizeof hdr, 1, f) == 1 && hdr[0] == kMagic;
-  // version 1: 16 features (no tensor-core flag); its weights are widened
-  // with a zero column, so it scores every pass as an FP32-pipe pass
   const uint32_t in = ok ? hdr[2] : 0;
-  ok = ok && ((hdr[1] == kVersion && in == (uint32_t)kMlpIn) || (hdr[1] == 1 && in == 16));
+  ok = ok && hdr[1] == kVersion && in == (uint32_t)kMlpIn;
   const uint32_t np = kMlpHidden * in + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden + kMlpHidden + 1;
   ok = ok && hdr[3] == np;
   CostModel t;
@@ -129,11 +130,13 @@ bool cost_model_train(CostModel& m, const std::vector<float>& X, const std::vect
     err = "empty or mismatched training set";
     return false;
   }
-  // standardised log-time targets
+  // standardised targets: log of the time per state entry (the time of a
+  // pass grows with the 4^n entries it sweeps; taking that out keeps the
+  // network's job size-independent, so it extrapolates across qubit counts)
   std::vector<float> T(B);
   double mean = 0, var = 0;
   for (int i = 0; i < B; i++) {
-    T[i] = std::log(std::max(ms[i], 1e-6f));
+    T[i] = (float)(std::log(std::max(ms[i], 1e-6f)) - log_entries(&X[(size_t)i * kMlpIn]));
     mean += T[i];
   }
   mean /= B;
@@ -217,7 +220,7 @@ bool cost_model_predict(const CostModel& m, const std::vector<float>& X, std::ve
   cudaStreamSynchronize(s);
   cudaStreamDestroy(s);
   if (!ok) return false;
-  for (float& v : ms) v = std::exp(v * m.y_std + m.y_mean);
+  for (int i = 0; i < B; i++) ms[i] = (float)std::exp(ms[i] * m.y_std + m.y_mean + log_entries(&X[(size_t)i * kMlpIn]));
   return true;
 }
 

@@ -21,6 +21,8 @@ struct CostModel {
 };
 
 CostModel& global_cost_model();
+// ln of the state entries a pass sweeps, from its features
+double log_entries(const float* x);
 // Held while the process-wide model is trained, loaded, saved or read.
 std::mutex& cost_model_mutex();
 bool cost_model_save(const CostModel& m, const std::string& path);
