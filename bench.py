@@ -9,7 +9,9 @@ Extra keys: the plain path's time and the speed-up, the fused-vs-plain error
 (the plain path checks every fused result), the roofline of the dominant pass
 kernel, ``e2e`` through the C ABI with host buffers (the circuit and rho cross
 the host boundary every step), and a CPU baseline of the reference's CPU
-algorithm (the oracle port, all host cores) on a bounded prefix sample.
+algorithm (the oracle port, all host cores) on a bounded systematic sample of
+the circuit at full size, with the fused result checked against the
+statevector oracle in that CPU leg.
 
     python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl reference]
                     [--n 14] [--gates 2000] [--planner greedy|learned] [--max-k 4]
@@ -103,48 +105,110 @@ def workload(n, gates):
     return W.table_mix(n, gates, seed=2)
 
 
-def cpu_sample(n, circ, budget_s, threads):
-    """Time the reference's CPU algorithm (oracle port) on a prefix of the
-    circuit at full size and extrapolate per basic gate.  Returns seconds per
-    circuit and a description of the sample."""
+METRIC = "14/16q circuit time, learned-fused vs plain on 1 GB300 at <=1e-10 err; HBM %"
+
+
+def cpu_stratified(n, circ, stride, offset, threads, fixed_s):
+    """Time the reference's CPU algorithm (the oracle port of
+    src/dmsim_cpu_omp.hpp) at full size on the systematic sample
+    circ[offset::stride] -- every stride-th table gate, so the sample has the
+    circuit's mix of basic gates -- and extrapolate to the whole circuit:
+    fixed_s (state set-up and the adjoint stage, timed on an empty circuit)
+    plus the sample's time per basic gate times the circuit's basic gates.
+    Returns (seconds per circuit, seconds the sample took, description)."""
+    import oracle as O
+    total_basic = sum(O.basic_count(g) for g in circ)
+    pre = circ[offset::stride]
+    nb = sum(O.basic_count(g) for g in pre)
+    t0 = time.perf_counter()
+    O.dm_sim(n, pre, nthreads=threads)
+    t = time.perf_counter() - t0
+    per_basic = max(t - fixed_s, 0.0) / max(nb, 1)
+    return fixed_s + per_basic * total_basic, t, \
+        f"every {stride}th gate from gate {offset} ({len(pre)} of {len(circ)} gates, {nb} of {total_basic} basic " \
+        f"gates) at n={n}, {t:.1f} s, plus {fixed_s:.1f} s fixed (empty circuit), extrapolated per basic gate"
+
+
+def cpu_fixed_cost(n, threads):
+    """Seconds of the reference CPU algorithm's per-run work that does not
+    depend on the gates: the state set-up and the adjoint (transpose) stage."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
+    t0 = time.perf_counter()
+    O.dm_sim(n, [], nthreads=threads)
+    return time.perf_counter() - t0
+
+
+def cpu_stride(n, circ, budget_s):
+    """Sampling stride so that one sample takes about budget_s at n qubits
+    (measured rate of the oracle port: ~27 ms per basic gate at 14 qubits on
+    16 Arm cores, scaling with 4^n)."""
+    per_basic = 0.027 * 4.0 ** (n - 14) * 16.0 / max(os.cpu_count() or 1, 1)
+    import oracle as O
     total_basic = sum(O.basic_count(g) for g in circ)
-    # grow the prefix until the sample takes ~budget_s
-    k = 1
-    t = 0.0
-    nb = 0
-    while True:
-        pre = circ[:k]
-        nb = sum(O.basic_count(g) for g in pre)
-        t0 = time.perf_counter()
-        O.dm_sim(n, pre, nthreads=threads)
-        t = time.perf_counter() - t0
-        if t >= budget_s / 3 or k >= len(circ):
-            break
-        k = min(len(circ), max(k + 1, int(k * max(2.0, budget_s / 3 / max(t, 1e-3)))))
-    per_basic = t / max(nb, 1)
-    return per_basic * total_basic, f"first {k} of {len(circ)} gates ({nb} of {total_basic} basic gates) at n={n}, " \
-                                    f"{t:.1f} s, extrapolated per basic gate"
+    want = max(1.0, budget_s / per_basic)
+    return max(1, int(round(total_basic / want)))
 
 
 def run_reference_arm(args, n, circ):
+    """The reference's own CPU algorithm for this path on the machine's host cores:
+    each step times one bounded systematic sample of the circuit at full size
+    (a different offset per step, so the steps together cover much of it) and
+    extrapolates to the whole circuit.  value = mean extrapolated seconds per
+    circuit; ms_per_step = the measured time of one step's sample."""
     threads = os.cpu_count() or 1
-    value, sample = cpu_sample(n, circ, args.cpu_budget, threads)
-    vals = [value]
-    for _ in range(max(0, args.steps - 1)):
-        v, _ = cpu_sample(n, circ, args.cpu_budget, threads)
+    fixed = cpu_fixed_cost(n, threads)
+    stride = cpu_stride(n, circ, args.cpu_budget)
+    for w in range(args.warmup):
+        cpu_stratified(n, circ[: 2 * stride], stride, 0, threads, fixed)  # small: page in and spin up threads
+    vals, times, samples = [], [], []
+    for k in range(args.steps):
+        v, t, sample = cpu_stratified(n, circ, stride, (k * 7) % stride, threads, fixed)
         vals.append(v)
+        times.append(t)
+        samples.append(sample)
     v = float(np.mean(vals))
-    line = {"impl": "reference", "metric": f"{n}q mixed-gate circuit time (reference CPU algorithm)", "value": v,
+    line = {"impl": "reference", "metric": METRIC, "value": v,
             "unit": "s/circuit", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": f"table_mix n={n} gates={len(circ)} seed=2", "l2": "inputs larger than L2"},
-            "cpu_baseline": {"value": v, "unit": "s/circuit", "cores": threads, "kind": "port", "sample": sample},
+            "ms_per_step": float(np.mean(times)) * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded circuits, state from |0..0><0..0|)",
+            "config": {"workload": f"{n}-qubit mixed-gate circuit: table_mix n={n} gates={len(circ)} seed=2 "
+                                   f"(29-entry table, random distinct qubits)", "l2": "inputs larger than L2",
+                       "step": "one systematic sample of the circuit at full size, extrapolated per basic gate; "
+                               "ms_per_step is the sample's measured time"},
+            "value_spread": [float(np.min(vals)), float(np.max(vals))],
+            "cpu_baseline": {"value": v, "unit": "s/circuit", "cores": threads, "kind": "port",
+                             "cpu": cpu_model(), "sample": samples[0] + f" (step 1 of {args.steps}; offsets vary)"},
             "e2e": {"value": v, "unit": "s/circuit", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def oracle_parity(n, circ, sim):
+    """The fused result against the statevector oracle (rho = psi psi^+ for
+    these noise-free circuits from a pure state), on the device: fidelity,
+    sqrt(1 - F) (an upper bound of the trace distance), max element and
+    Frobenius errors.  Part of the CPU leg: the oracle is the checker here."""
+    import oracle as O
+    sr, si = O.sv_sim(n, circ)
+    sim.reset_dm()
+    sim.run()
+    m = sim.pure_metrics(sr + 1j * si)
+    m["sqrt_1_minus_F"] = float(np.sqrt(max(0.0, 1.0 - m["fidelity"])))
+    return m
+
+
+def cpu_model():
+    try:
+        with open("/proc/cpuinfo") as f:
+            txt = f.read()
+        for key in ("model name", "CPU part", "Hardware"):
+            for ln in txt.splitlines():
+                if ln.startswith(key):
+                    return f"{key}: {ln.split(':', 1)[1].strip()} ({os.cpu_count()} cores, {os.uname().machine})"
+    except OSError:
+        pass
+    return f"{os.uname().machine}, {os.cpu_count()} cores"
 
 
 def class_profile(sim, arith_name):
@@ -301,7 +365,8 @@ def main():
     ap.add_argument("--planner", default="learned")
     ap.add_argument("--max-k", type=int, default=4)
     ap.add_argument("--tensor", default="1", help="tensor-core passes: 0 off, 1 planner's choice, all")
-    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--cpu-budget", type=float, default=None,
+                    help="seconds per CPU sample [20 for the cpu_baseline leg, 8 per step of --impl reference]")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
@@ -316,6 +381,8 @@ def main():
     n = args.n
     circ = workload(n, args.gates)
 
+    if args.cpu_budget is None:
+        args.cpu_budget = 8.0 if args.impl == "reference" else 20.0
     if args.impl == "reference":
         if rank == 0:
             run_reference_arm(args, n, circ)
@@ -425,16 +492,20 @@ def main():
     pim.close()
 
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, sample = cpu_sample(n, circ, args.cpu_budget, threads)
-        cpu = {"value": v, "unit": "s/circuit", "cores": threads, "kind": "port", "sample": sample}
+        fixed = cpu_fixed_cost(n, threads)
+        v, _, sample = cpu_stratified(n, circ, cpu_stride(n, circ, args.cpu_budget), 0, threads, fixed)
+        cpu = {"value": v, "unit": "s/circuit", "cores": threads, "kind": "port", "cpu": cpu_model(),
+               "sample": sample}
+        parity = oracle_parity(n, circ, fused)
 
     if rank == 0:
         # whole-job aggregate: the world's ranks each ran one circuit per step
         value = step_ms / 1e3 / world
         line = {
-            "metric": "14/16q circuit time, learned-fused vs plain on 1 GB300 at <=1e-10 err; HBM %",
+            "metric": METRIC,
             "value": value, "unit": "s/circuit", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "df64", "data": "synthetic (seeded circuits, state from |0..0><0..0|)",
@@ -466,6 +537,7 @@ def main():
             "upload_s": upload_s,
             "wall_s_timed": wall,
             "cpu_baseline": cpu,
+            "parity_vs_statevector_oracle": parity,
         }
         print(json.dumps(line))
     fused.close()

@@ -336,7 +336,16 @@ int dmsim_batch_run(dmsim_batch_handle b) {
     b->last_ms = ms;
     int err = 0;
     B_CUDA(cudaMemcpy(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (err) throw BErr{DMSIM_ERR_TIMEOUT, "a work-queue dependency wait ran out; results are incomplete"};
+    if (err) {
+      // Items after the expired wait ran on partly updated states: make every
+      // output NaN (all-ones bytes) rather than leave plausible values behind.
+      B_CUDA(cudaMemsetAsync(b->d_diag, 0xFF, b->diag_total * sizeof(double), b->stream));
+      B_CUDA(cudaMemsetAsync(b->d_zz, 0xFF, b->zz_total * sizeof(double), b->stream));
+      B_CUDA(cudaMemsetAsync(b->d_re, 0xFF, b->total_entries * sizeof(double), b->stream));
+      B_CUDA(cudaMemsetAsync(b->d_im, 0xFF, b->total_entries * sizeof(double), b->stream));
+      B_CUDA(cudaStreamSynchronize(b->stream));
+      throw BErr{DMSIM_ERR_TIMEOUT, "a work-queue dependency wait ran out; every output of this run is NaN"};
+    }
   });
 }
 

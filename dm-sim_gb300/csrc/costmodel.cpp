@@ -248,10 +248,11 @@ std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int 
   // double-float state only: at 17 qubits the model (trained up to 16) picked
   // complex64 tensor passes that ran slower than the FP32 pipe (71.4 s against
   // 62.5 s for the circuit); complex64 tensor passes stay opt-in (option 2)
-  const bool tc_ok = tensor && arith == 2;
+  // FP64 state: the FP64-width tensor passes (tensor64.cu)
+  const bool tc_ok = tensor && (arith == 2 || arith == 0);
   auto work = [&](Cand& c) {
     c.plan = c.k == 1 ? plan_plain(basics) : plan_greedy(basics, c.k, c.cap);
-    std::vector<unsigned char> buf(std::max(desc_size(kMaxK), tc_desc_bytes(kMaxK)));
+    std::vector<unsigned char> buf(std::max(desc_size(kMaxK), std::max(tc_desc_bytes(kMaxK, 2), tc_desc_bytes(kMaxK, 0))));
     for (size_t i = 0; i < c.plan.size(); i++) {
       const PassSpec& p = c.plan[i];
       if (p.transpose) continue;
@@ -260,7 +261,7 @@ std::vector<PassSpec> plan_learned(const std::vector<Basic>& basics, int n, int 
         PassFeatures f;
         std::memset(&f, 0, sizeof f);
         if (v == 0) build_desc(p, n, buf.data(), &f, nullptr, nullptr);
-        else build_tc_desc(p, n, buf.data(), &f, nullptr, nullptr, false);
+        else build_tc_desc(p, n, buf.data(), &f, nullptr, nullptr, false, arith);
         f.arith = arith;
         f.tc = v;
         float x[kMlpIn];

@@ -267,7 +267,7 @@ void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_b
     offs.push_back(total);
     const bool tc = use_tensor(s, p, arith);
     tcs.push_back(tc);
-    if (!p.transpose) total += ((tc ? tc_desc_bytes(p.K) : desc_size(p.K)) + 255) & ~(size_t)255;
+    if (!p.transpose) total += ((tc ? tc_desc_bytes(p.K, arith) : desc_size(p.K)) + 255) & ~(size_t)255;
   }
   std::vector<unsigned char> blob(std::max<size_t>(total, 256));
   s->passes.clear();
@@ -295,7 +295,7 @@ void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_b
     int tile = 0;
     pi.tc = tcs[i] != 0;
     const uint64_t entries =
-        pi.tc ? build_tc_desc(specs[i], (int)s->n, blob.data() + offs[i], &pi.feat, &ntiles, &tile)
+        pi.tc ? build_tc_desc(specs[i], (int)s->n, blob.data() + offs[i], &pi.feat, &ntiles, &tile, true, arith)
               : build_desc(specs[i], (int)s->n, blob.data() + offs[i], &pi.feat, &ntiles, &tile);
     pi.feat.tc = pi.tc ? 1 : 0;
     pi.real = !pi.tc && pi.feat.real;
@@ -1133,7 +1133,7 @@ int dmsim_cost_collect(uint32_t n, uint32_t n_circuits, uint32_t gates, uint64_t
           for (const PassSpec& p : specs) any_tc |= tc_eligible(p, (int)n);
           // double-float plans are timed on the FP32 pipe and, where passes
           // can run there, on the tensor cores
-          const int variants = ((arith == AR_DF64 || arith == AR_FP32) && any_tc) ? 2 : 1;
+          const int variants = any_tc ? 2 : 1;
           for (int v = 0; v < variants; v++) {
             h->tensor = v == 1 ? 2 : 0;
             upload_specs(h, specs, (uint32_t)basics.size(), arith);

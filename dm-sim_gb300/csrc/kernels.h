@@ -18,7 +18,8 @@ struct LaunchArgs {
   unsigned grid;       // blocks
   int tile_entries;    // G * 4^K
   bool real;           // DENSE/SPARSE pass whose U and V are real (pass.h kPassRealOperator)
-  bool tc;             // tensor-core pass (desc is a TcDesc<K>; double-float or FP32 state, K = 3, 4)
+  bool tc;             // tensor-core pass, K = 3, 4: desc is a TcDesc<K> (double-float or FP32 state) or,
+                       // for an FP64 state, a TcDesc64<K>
   int* err;            // device flag set to 1 when a bounded wait of a tensor pass runs out
   bool direct1;        // 1-qubit pass run by the register kernel (kernels_k1.cu)
   int q0, n;           // its qubit and the state's qubit count
@@ -36,6 +37,9 @@ cudaError_t launch_pass_real(const LaunchArgs& a, cudaStream_t s);
 // Tensor-core passes (tensor.cu): launch, and resident blocks per SM.
 cudaError_t launch_pass_tc(const LaunchArgs& a, cudaStream_t s);
 int tc_blocks_per_sm(int K, int arith);
+// FP64-width tensor-core passes on an FP64 state (tensor64.cu): one
+// persistent 512-thread block per SM.
+cudaError_t launch_pass_tc64(const LaunchArgs& a, cudaStream_t s);
 // In place: FP64 entries <-> double-float pairs (the fused path's working format)
 cudaError_t launch_to_df64(void* re, void* im, uint64_t N, unsigned grid, cudaStream_t s);
 cudaError_t launch_from_df64(void* re, void* im, uint64_t N, unsigned grid, cudaStream_t s);

@@ -111,6 +111,28 @@ DMG_HD constexpr uint32_t tc_kmajor_offset(uint32_t row, uint32_t k, uint32_t sb
   return (row >> 3) * sbo + (k >> 3) * 128u + (row & 7) * 16u + (k & 7) * 2u;
 }
 
+// ---- FP64-width tensor-core passes (K = 3, 4; FP64 state)
+// Every operand value is an integer on a power-of-two grid, split into 7
+// balanced base-256 digits (|digit| <= 128, exact in BF16): 55 significant
+// bits for the largest value of each column of the state, 56 for each row
+// of the operator.  Slice pairs of orders i + j = 0..7 accumulate exactly in
+// FP32 (every partial sum is an integer below 2^22), the orders are combined
+// in 64-bit integer arithmetic and rounded once to FP64.
+constexpr int kTc64Slices = 7;
+constexpr int kTc64Orders = 8;
+
+template <int K>
+struct TcDesc64 {
+  static constexpr int D = 1 << K, R = 2 * D;
+  PassHeader h;  // tile geometry, g = 7 - K (128 columns per step)
+  // Row exponents: row n of W (0) or V (1) equals 2^ew[side][n mod D] times
+  // sum_j digit_j 256^(6-j); rows n and n + D (the real and imaginary parts
+  // of output n) hold the same magnitudes and share the exponent.
+  int32_t ew[2][D];
+  // digits j = 0..6 of W (0) and V (1): BF16 bits, K-major core-matrix layout
+  alignas(16) uint16_t sl[2][kTc64Slices][R * R];
+};
+
 template <int K>
 struct TcDesc {
   static constexpr int D = 1 << K, R = 2 * D;

@@ -575,8 +575,68 @@ uint64_t build_tc_k(const PassSpec& p, int n, TcDesc<K>* d, PassFeatures* feat, 
   return (uint64_t)(nst + nruns) * runlen * h.ntiles;
 }
 
+void tc64_digits(int64_t t, int d[7]) {
+  // u = t + 0x80 in every byte: each byte of u minus 0x80 is a balanced digit
+  const uint64_t u = (uint64_t)t + 0x0080808080808080ull;
+  for (int j = 1; j < 7; j++) d[j] = (int)((u >> (8 * (6 - j))) & 0xFF) - 128;
+  d[0] = (int)(u >> 48) - 128;
+}
+
+// The FP64-width descriptor: the geometry of the double-float tensor pass and
+// the operator's rows as 56-bit integers times a power of two, in digits.
+template <int K>
+uint64_t build_tc64_k(const PassSpec& p, int n, TcDesc64<K>* d, PassFeatures* feat, uint64_t* ntiles_out,
+                      int* tile_out, bool slices) {
+  constexpr int D = 1 << K, R = 2 * D;
+  std::unique_ptr<PassDesc<K>> geo(new PassDesc<K>);
+  build_k<K>(p, n, geo.get(), feat, ntiles_out, tile_out, 7 - K);
+  std::memset(d, 0, sizeof(*d));
+  d->h = geo->h;
+  PassHeader& h = d->h;
+  const int nruns = 1 << h.mhi;
+  int nst = 0;
+  for (int r = 0; r < nruns; r++) {
+    h.ldmask[r >> 5] |= 1u << (r & 31);
+    nst += (h.stmask[r >> 5] >> (r & 31)) & 1;
+  }
+  if (feat) feat->ld_frac = 1.0;
+  for (int side = 0; side < 2 && slices; side++) {
+    const cplx* M = side ? p.V : p.U;
+    for (int a = 0; a < D; a++) {
+      // rows a ([Ur, -Ui]) and a + D ([Ui, Ur]) hold the same magnitudes
+      double mx = 0;
+      for (int k = 0; k < D; k++) mx = std::max(mx, std::max(std::fabs(M[a * D + k].real()), std::fabs(M[a * D + k].imag())));
+      int e = 0;
+      if (mx > 0) std::frexp(mx, &e);  // every |entry| < 2^e
+      d->ew[side][a] = mx > 0 ? e - 55 : 0;
+      for (int half = 0; half < 2; half++) {
+        const int row = a + half * D;
+        for (int k = 0; k < R; k++) {
+          const cplx m = M[a * D + (k % D)];
+          const double w = half == 0 ? (k < D ? m.real() : -m.imag()) : (k < D ? m.imag() : m.real());
+          const int64_t t = mx > 0 ? (int64_t)std::nearbyint(std::ldexp(w, 55 - e)) : 0;  // |t| <= 2^55
+          int dg[7];
+          tc64_digits(t, dg);
+          for (int j = 0; j < kTc64Slices; j++) {
+            const float tf = (float)dg[j];  // |digit| <= 128: exact in BF16
+            uint32_t bits;
+            std::memcpy(&bits, &tf, 4);
+            d->sl[side][j][tc_kmajor_offset(row, k, 16 * R) / 2] = (uint16_t)(bits >> 16);
+          }
+        }
+      }
+    }
+  }
+  const uint64_t runlen = 1ull << h.L;
+  return (uint64_t)(nst + nruns) * runlen * h.ntiles;
+}
+
 uint64_t build_tc_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries,
-                       bool slices) {
+                       bool slices, int arith) {
+  if (arith == 0) {
+    if (p.K == 3) return build_tc64_k<3>(p, n, static_cast<TcDesc64<3>*>(out), f, ntiles, tile_entries, slices);
+    return build_tc64_k<4>(p, n, static_cast<TcDesc64<4>*>(out), f, ntiles, tile_entries, slices);
+  }
   if (p.K == 3) return build_tc_k<3>(p, n, static_cast<TcDesc<3>*>(out), f, ntiles, tile_entries, slices);
   return build_tc_k<4>(p, n, static_cast<TcDesc<4>*>(out), f, ntiles, tile_entries, slices);
 }
@@ -590,14 +650,18 @@ bool tc_eligible(const PassSpec& p, int n) {
 }
 
 bool tc_choose(const PassSpec& p, int n, int tensor_opt, int arith) {
-  if (!tensor_opt || (arith != 2 && arith != 1) || !tc_eligible(p, n)) return false;  // double-float or FP32 state
+  if (!tensor_opt || !tc_eligible(p, n)) return false;
   if (tensor_opt == 2) return true;  // every eligible pass (measurements)
-  if (arith != 2) return false;      // complex64: opt-in only (option 2)
+  if (arith == 1) return false;      // complex64: opt-in only (option 2)
   if (p.tc >= 0) return p.tc != 0;   // the learned planner's choice
+  if (arith == 0) return true;       // FP64: the alternative is GB300's FP64 pipe
   return p.nnz >= kTcMinRowNnz * (1 << p.K);
 }
 
-size_t tc_desc_bytes(int K) { return K == 3 ? sizeof(TcDesc<3>) : sizeof(TcDesc<4>); }
+size_t tc_desc_bytes(int K, int arith) {
+  if (arith == 0) return K == 3 ? sizeof(TcDesc64<3>) : sizeof(TcDesc64<4>);
+  return K == 3 ? sizeof(TcDesc<3>) : sizeof(TcDesc<4>);
+}
 
 uint64_t build_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries,
                     int g_cap) {

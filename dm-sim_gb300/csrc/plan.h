@@ -74,10 +74,15 @@ bool tc_eligible(const PassSpec& p, int n);
 // kTcMinRowNnz nonzeros per row of U (the tensor cores' cost does not depend
 // on the density, the FP32-pipe kernel's grows with it).
 constexpr int kTcMinRowNnz = 3;
+// arith: the run's arithmetic (kernels.h Arith: 0 FP64, 1 FP32, 2 double-float).
+// FP64 runs use the FP64-width passes (TcDesc64), the others TcDesc.
 bool tc_choose(const PassSpec& p, int n, int tensor_opt, int arith);
-size_t tc_desc_bytes(int K);
+size_t tc_desc_bytes(int K, int arith = 2);
 // slices = false: geometry and features only (the planner's scoring).
 uint64_t build_tc_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries,
-                       bool slices = true);
+                       bool slices = true, int arith = 2);
+// The 7 balanced base-256 digits of an integer |t| <= 2^55 (digit 0 the most
+// significant, weight 256^(6-j)): t = sum_j d[j] 256^(6-j), |d[j]| <= 128.
+void tc64_digits(int64_t t, int d[7]);
 
 }  // namespace dmg

@@ -234,8 +234,15 @@ __device__ bool tc_step(T* __restrict__ sre, T* __restrict__ sim, unsigned char*
     tc::mma_commit(&tb.bar);
   }
   const bool done = tc::mbar_wait_bounded(&tb.bar, phase, 1u << 24);
+  if (!__syncthreads_and(done)) {
+    // The commit did not arrive in time.  The caller releases the tensor
+    // memory next, which the MMAs already issued may still write: give them
+    // one more, longer, bounded wait first.  The pass has failed either way
+    // (the host reports DMSIM_ERR_TIMEOUT and the state is undefined).
+    tc::mbar_wait_bounded(&tb.bar, phase, 1u << 26);
+    return false;
+  }
   phase ^= 1u;
-  if (!__syncthreads_and(done)) return false;
   tc::fence_after_sync();
   after_mma();
 
@@ -492,6 +499,7 @@ static int tc_occ() {
 }
 
 int tc_blocks_per_sm(int K, int arith) {
+  if (arith == AR_FP64) return 1;  // the FP64-width kernel: one persistent block per SM (tensor64.cu)
   if (arith == AR_FP32) return K == 3 ? tc_occ<3, float>() : tc_occ<4, float>();
   return K == 3 ? tc_occ<3, df64>() : tc_occ<4, df64>();
 }

@@ -1,0 +1,532 @@
+// tensor64.cu -- dense K = 3, 4 qubit passes on the tensor cores for an FP64
+// state, at FP64 width, with no FP64 instruction (GB300's FP64 pipe and its
+// FP64 conversions run at ~1/60 of the FP32 rate).
+//
+// A pass is two products per tile, as in the double-float tensor pass: the
+// ket step multiplies every tile column x (2^K complex entries as R = 2^(K+1)
+// reals) by the real embedding W = [[Ur, -Ui], [Ui, Ur]], the bra step the
+// result's columns by V.  Here every operand value is an integer times a
+// power of two, split into 7 balanced base-256 digits (|digit| <= 128, exact
+// in BF16):
+//   * a state column (ket step): the FP64 bits are aligned in integer
+//     arithmetic to the column's largest exponent, v = |x| 2^(1077 - Ec) <
+//     2^55 (55 significant bits for the column's largest value);
+//   * an operator row (host, TcDesc64): w = t 2^ew with |t| <= 2^55;
+//   * a bra-step column: the ket step's exact integer outputs, aligned to the
+//     bra column's own magnitude (54-55 significant bits for its largest).
+// Digit pairs of orders i + j = 0..7 are summed by tcgen05.mma into one FP32
+// accumulator per order; every partial sum is an integer below 7 R 2^14 <=
+// 2^22, so the sums are exact.  The orders are combined in 64-bit integer
+// arithmetic (orders 6 and 7 below 2^-40 of order 0 enter through one
+// truncating shift) and the bra step's result is rounded once to FP64 (round
+// half up) from the 64-bit integer.  Error per step: below 2^-54 of the
+// column's largest value times the operator row's largest entry, per term;
+// FP64 dot products of the same length carry about 2^-53 per term.
+//
+// Threads: 512 (16 warps), one block per SM.  Thread (warp w, lane l) owns
+// tile column m = 32 (w & 3) + l -- the TMEM lane its warp may read -- and
+// quarter q = w >> 2 of it: R/4 consecutive values (real parts for q < 2,
+// imaginary parts for q >= 2).  Per tile:
+//   1. wait for the tile (TMA bulk copies of its runs, issued two tiles ahead)
+//   2. ket digits -> A_ket;  3. one thread issues the ket MMAs (TMEM set t&1)
+//   4. the previous tile's bra accumulators -> FP64 -> global stores,
+//      overlapping the ket MMAs
+//   5. ket accumulators -> exact int64 outputs in the tile buffer
+//   6. bra digits -> A_bra;  7. one thread issues the bra MMAs (same set)
+//   8. warp 0 starts the loads of the tile two ahead into the freed buffer;
+//      the bra MMAs overlap the next tile's steps 1-3.
+// Every wait is bounded; on expiry the block sets the error flag, waits
+// (bounded) for its own copies and MMAs in flight, releases its TMEM and
+// returns, and the host reports DMSIM_ERR_TIMEOUT.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels.h"
+#include "pass_device.cuh"
+#include "tc.cuh"
+
+namespace dmg {
+
+namespace {
+
+constexpr int kT64Threads = 512;
+constexpr uint32_t kT64WaitPolls = 1u << 24;
+
+template <int K>
+struct T64 {
+  static constexpr int D = 1 << K, R = 2 * D, G = 128 / D, TILE = 128 * D;
+  static constexpr int Q = R / 4;                          // values of one column per thread
+  static constexpr uint32_t SBO = 16 * R;                  // bytes between 8-row groups of an R-wide operand
+  static constexpr uint32_t A_BYTES = 128 * R * 2;         // one digit slice of the 128 columns
+  static constexpr uint32_t B_BYTES = R * R * 2;           // one digit slice of W or V
+  static constexpr uint32_t SET_COLS = kTc64Orders * R;    // accumulators of one step
+  static constexpr uint32_t TMEM_COLS = 2 * SET_COLS;      // two sets: 512 (K = 4), 256 (K = 3)
+  static constexpr uint32_t BUF_BYTES = TILE * 8 * 2;      // one tile, re + im, 8 bytes per real
+  static_assert(TMEM_COLS <= 512, "two accumulator sets must fit in tensor memory");
+};
+
+template <int K>
+struct T64Tables {
+  static constexpr int D = 1 << K;
+  uint64_t hioff[256];
+  uint64_t full[2];       // tile loads into buffer 0 / 1
+  uint64_t mma[2];        // commits of the ket (0) and bra (1) products
+  uint32_t stmask[8];
+  int lk[D], lb[D];
+  int ew[2][D];
+  uint32_t colmax[4][128];  // per quarter and column: largest FP64 exponent field
+  uint32_t brmax[2][128];   // per tile parity and bra column: magnitude key of the ket outputs
+  int colE[128];            // biased exponent of each ket column's grid
+  uint32_t slot;
+  int abort_;
+};
+
+template <int K>
+constexpr size_t t64_smem_bytes() {
+  using S = T64<K>;
+  return 2 * (size_t)kTc64Slices * S::A_BYTES + 2 * (size_t)kTc64Slices * S::B_BYTES + 2 * (size_t)S::BUF_BYTES +
+         sizeof(T64Tables<K>);
+}
+
+__device__ __forceinline__ uint64_t shr_u64(uint64_t x, uint32_t s) {  // s >= 64 gives 0
+  uint64_t r;
+  asm("shr.b64 %0, %1, %2;" : "=l"(r) : "l"(x), "r"(s));
+  return r;
+}
+__device__ __forceinline__ int64_t shr_s64(int64_t x, uint32_t s) {  // s >= 64 gives the sign
+  int64_t r;
+  asm("shr.s64 %0, %1, %2;" : "=l"(r) : "l"(x), "r"(s));
+  return r;
+}
+__device__ __forceinline__ int64_t shl_s64(int64_t x, uint32_t s) {
+  int64_t r;
+  asm("shl.b64 %0, %1, %2;" : "=l"(r) : "l"(x), "r"(s));
+  return r;
+}
+
+// Byte-permute selectors: float bits 0x4B0000bb (= 2^23 + bb) from byte k of
+// a word, and 0x4B00hhbb from its bytes 2, 3 (the top digit's 9 bits).
+constexpr uint32_t kMagicHi = 0x4B000000u;
+__device__ __forceinline__ float byte_float(uint32_t x, uint32_t sel) {
+  return __uint_as_float(__byte_perm(x, kMagicHi, sel));
+}
+
+// The 7 digits (digit 0 the most significant) of the balanced base-256
+// representation of u - B, B = 0x80 in bytes 0..6, each times s and shifted
+// by c: digit j = (byte_{6-j}(u) - 128) s, the top one from bits 48..56.
+__device__ __forceinline__ void digits_of(uint64_t u, float s, float c, float (&dg)[kTc64Slices]) {
+  const uint32_t ul = (uint32_t)u, uh = (uint32_t)(u >> 32);
+  dg[6] = fmaf(byte_float(ul, 0x7540), s, c);
+  dg[5] = fmaf(byte_float(ul, 0x7541), s, c);
+  dg[4] = fmaf(byte_float(ul, 0x7542), s, c);
+  dg[3] = fmaf(byte_float(ul, 0x7543), s, c);
+  dg[2] = fmaf(byte_float(uh, 0x7540), s, c);
+  dg[1] = fmaf(byte_float(uh, 0x7541), s, c);
+  dg[0] = fmaf(byte_float(uh, 0x7532), s, c);
+}
+constexpr uint64_t kDigitBias = 0x0080808080808080ull;
+
+// Digits of an FP64 value (bits lo, hi) on its column's grid: ecm is the
+// column's largest exponent field (hi & 0x7FF00000, at least 64 << 20).
+// v = |x| 2^(1077 - Ec) = (mantissa << 2) >> (Ec - E) < 2^55; the sign is
+// applied to every digit.  Zeros and subnormals (exponent field 0) shift out.
+__device__ __forceinline__ void digits_fp64(uint32_t lo, uint32_t hi, uint32_t ecm, float (&dg)[kTc64Slices]) {
+  const uint32_t d = (ecm - (hi & 0x7FF00000u)) >> 20;
+  const uint64_t mant = ((uint64_t)((hi & 0x000FFFFFu) | 0x00100000u) << 32) | lo;
+  const uint64_t u = shr_u64(mant << 2, d) + kDigitBias;
+  const uint32_t sgn = hi & 0x80000000u;
+  digits_of(u, __uint_as_float(sgn | 0x3F800000u), __uint_as_float(sgn ^ 0xCB000080u), dg);  // +-1, -+(2^23 + 128)
+}
+
+// Digits of a signed integer |v| < 2^55.
+__device__ __forceinline__ void digits_int(int64_t v, float (&dg)[kTc64Slices]) {
+  digits_of((uint64_t)v + kDigitBias, 1.0f, -8388736.0f, dg);  // -(2^23 + 128)
+}
+
+// Y = sum_o S_o 2^(8(5-o)) for o <= 5, plus floor((S_6 2^8 + S_7) / 2^16),
+// from the exact integer order sums S_o (|S_o| < 2^22, held in FP32): S + 1.5
+// 2^23 has the bits 0x4B400000 + S.
+__device__ __forceinline__ int64_t combine_orders(float s0, float s1, float s2, float s3, float s4, float s5,
+                                                  float s6, float s7) {
+  constexpr float M = 12582912.0f;
+  constexpr uint32_t K257 = 257u * 0x4B400000u;  // mod 2^32
+  const uint32_t b0 = __float_as_uint(s0 + M), b1 = __float_as_uint(s1 + M), b2 = __float_as_uint(s2 + M),
+                 b3 = __float_as_uint(s3 + M), b4 = __float_as_uint(s4 + M), b5 = __float_as_uint(s5 + M),
+                 b6 = __float_as_uint(s6 + M), b7 = __float_as_uint(s7 + M);
+  const int32_t p01 = (int32_t)((b0 << 8) + b1 - K257);  // S_0 2^8 + S_1, below 2^31 in magnitude
+  const int32_t p23 = (int32_t)((b2 << 8) + b3 - K257);
+  const int32_t p45 = (int32_t)((b4 << 8) + b5 - K257);
+  const int32_t p67 = (int32_t)((b6 << 8) + b7 - K257) >> 16;
+  return ((int64_t)p01 << 32) + ((int64_t)p23 << 16) + (int64_t)(p45 + p67);
+}
+
+// The FP64 bits of Y 2^P, rounded half up to 53 bits; 0 for Y = 0 or below
+// the normal range.
+__device__ __forceinline__ uint64_t to_fp64(int64_t Y, int P) {
+  const uint64_t s = (uint64_t)(Y >> 63);
+  const uint64_t a = ((uint64_t)Y ^ s) - s;
+  const int lz = __clzll((long long)a);
+  const uint64_t nrm = a << (lz & 63);
+  const uint64_t mant = (nrm >> 11) + ((nrm >> 10) & 1);  // 2^52 <= mant <= 2^53
+  const int E = 1086 - lz + P;                            // biased exponent of the value
+  const uint64_t bits = ((uint64_t)(E - 1) << 52) + mant + (s << 63);
+  return (a == 0 || E <= 0) ? 0ull : bits;
+}
+
+template <int Q>
+__device__ __forceinline__ void tmem_ld_q(uint32_t taddr, float (&v)[Q]) {
+  if constexpr (Q == 8) tc::tmem_ld8(taddr, v);
+  else tc::tmem_ld4(taddr, v);
+}
+
+// Pack Q digits of slice j (Q consecutive K indices of row m) into the
+// K-major operand: 16 bytes (Q = 8) or 8 bytes (Q = 4).
+template <int K>
+__device__ __forceinline__ void store_digits(unsigned char* sA, uint32_t off, const float (&dg)[T64<K>::Q][kTc64Slices]) {
+  using S = T64<K>;
+#pragma unroll
+  for (int j = 0; j < kTc64Slices; j++) {
+    uint32_t pk[S::Q / 2];
+#pragma unroll
+    for (int c = 0; c < S::Q; c += 2) {
+      const __nv_bfloat162 v = __floats2bfloat162_rn(dg[c][j], dg[c + 1][j]);  // exact: |digit| <= 128
+      pk[c >> 1] = *reinterpret_cast<const uint32_t*>(&v);
+    }
+    if constexpr (S::Q == 8)
+      *reinterpret_cast<uint4*>(sA + j * S::A_BYTES + off) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    else
+      *reinterpret_cast<uint2*>(sA + j * S::A_BYTES + off) = make_uint2(pk[0], pk[1]);
+  }
+}
+
+// One thread issues every product of a step: digit slices A_0..A_6 of the
+// 128 columns against the operator's slices, slice pairs of orders 0..7, the
+// pairs of order o into the accumulator at TMEM column o*R of the set.  The
+// operator's slices are consecutive R-row blocks of one K-major operand, so
+// A_i against slices j0..j0+nb-1 is one MMA of N = nb*R.
+template <int K>
+__device__ __forceinline__ void issue_step(const unsigned char* sA, const unsigned char* sBside, uint32_t dset) {
+  using S = T64<K>;
+  constexpr int R = S::R;
+  const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sBside);
+  auto issue = [&](int i, int j0, int nb, bool overwrite) {
+#pragma unroll
+    for (int kk = 0; kk < R / 16; kk++) {
+      const uint64_t ad = tc::smem_desc(a0 + i * S::A_BYTES + kk * 256, tc::kLbo, S::SBO);
+      const uint64_t bd = tc::smem_desc(b0 + j0 * S::B_BYTES + kk * 256, tc::kLbo, S::SBO);
+      tc::mma_bf16(dset + (i + j0) * R, ad, bd, tc::idesc_bf16_f32(128, nb * R), (overwrite && kk == 0) ? 0u : 1u);
+    }
+  };
+  issue(0, 0, 1, true);   // order 0
+  issue(1, 0, 7, true);   // (1, 0..6): orders 1..7
+  issue(0, 1, 6, false);  // (0, 1..6): orders 1..6
+#pragma unroll
+  for (int i = 2; i < kTc64Slices; i++) issue(i, 0, kTc64Orders - i, false);  // (i, 0..7-i)
+}
+
+}  // namespace
+
+template <int K>
+__global__ void __launch_bounds__(kT64Threads, 1)
+    k_pass_tc64(uint64_t* __restrict__ re, uint64_t* __restrict__ im, const TcDesc64<K>* __restrict__ dp,
+                int* __restrict__ err) {
+  using S = T64<K>;
+  constexpr int D = S::D, R = S::R, G = S::G, Q = S::Q, TILE = S::TILE;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* sAk = smem;
+  unsigned char* sAb = sAk + kTc64Slices * S::A_BYTES;
+  unsigned char* sB = sAb + kTc64Slices * S::A_BYTES;  // W digits, then V digits
+  uint64_t* bufs = reinterpret_cast<uint64_t*>(sB + 2 * kTc64Slices * S::B_BYTES);  // [buffer][re, im][TILE]
+  T64Tables<K>& tb = *reinterpret_cast<T64Tables<K>*>(bufs + 4 * TILE);
+  const PassHeader& h = dp->h;
+  const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
+  const int m = 32 * (w & 3) + l, q = w >> 2;
+  const int r = m / G, f = m & (G - 1);
+  const int c0 = q * Q;       // first value of this thread's quarter of a column
+  const int half = c0 / D;    // 0: real parts, 1: imaginary parts
+  const int cb = c0 % D;      // first ket (ket step) or bra (bra step) index of the quarter
+
+  // ---- per-pass tables, the operator's digits, tensor memory, barriers
+  {
+    constexpr int per_slice = S::B_BYTES / 16;
+    for (int i = tid; i < 2 * kTc64Slices * per_slice; i += blockDim.x) {
+      const int side = i / (kTc64Slices * per_slice), rest = i % (kTc64Slices * per_slice);
+      reinterpret_cast<uint4*>(sB)[i] = reinterpret_cast<const uint4*>(&dp->sl[side][0][0])[rest];
+    }
+  }
+  for (int run = tid; run < (1 << h.mhi); run += blockDim.x) {
+    uint64_t off = 0;
+    for (int j = 0; j < h.mhi; j++) off |= (uint64_t)((run >> j) & 1) << h.hipos[j];
+    tb.hioff[run] = off;
+  }
+  if (tid < 8) tb.stmask[tid] = h.stmask[tid];
+  if (tid < D) {
+    int lk = 0, lb = 0;
+    for (int i = 0; i < K; i++) {
+      lk |= ((tid >> i) & 1) << h.lket[i];
+      lb |= ((tid >> i) & 1) << h.lbra[i];
+    }
+    tb.lk[tid] = lk;
+    tb.lb[tid] = lb;
+    tb.ew[0][tid] = dp->ew[0][tid];
+    tb.ew[1][tid] = dp->ew[1][tid];
+  }
+  if (tid < 128) tb.brmax[0][tid] = tb.brmax[1][tid] = 0;
+  if (tid == 0) tb.abort_ = 0;
+  if (w == 0) {
+    tc::tmem_alloc(&tb.slot, S::TMEM_COLS);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(&tb.full[0], 1);
+    tc::mbar_init(&tb.full[1], 1);
+    tc::mbar_init(&tb.mma[0], 1);
+    tc::mbar_init(&tb.mma[1], 1);
+    tc::mbar_fence_init();
+  }
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tb.slot;
+  const uint32_t tlane = (uint32_t)(32 * (w & 3)) << 16;
+
+  int lf_g = 0;  // free-bit offset of this column's group f (the same in both steps)
+  for (int j = 0; j < h.g; j++) lf_g |= ((f >> j) & 1) << h.freepos[j];
+  const int L = h.L, runlen = 1 << L, nruns = 1 << h.mhi;
+  const uint64_t ntiles = h.ntiles, step = gridDim.x;
+
+  // warp 0: every run of tile t (real and imaginary arrays) into buffer b
+  auto load_tile = [&](uint64_t t, int b) {
+    uint64_t* dst = bufs + (size_t)b * 2 * TILE;
+    const uint64_t base = tile_base(h, t);
+    if (l == 0) {
+      tc::fence_proxy_async_smem();
+      tc::mbar_arrive_expect_tx(&tb.full[b], S::BUF_BYTES);
+    }
+    __syncwarp();
+    for (int i = l; i < 2 * nruns; i += 32) {
+      const int run = i >> 1, arr = i & 1;
+      const uint64_t* src = (arr ? im : re) + base + tb.hioff[run];
+      tc::bulk_g2s(dst + arr * TILE + run * runlen, src, (uint32_t)runlen * 8u, &tb.full[b]);
+    }
+  };
+
+  // outstanding asynchronous work, the same on every thread
+  uint32_t ph_full[2] = {0, 0}, ph_mma[2] = {0, 0};
+  int pend_full[2] = {0, 0}, pend_mma[2] = {0, 0};
+  bool timed_out = false;
+  // a phase that did not complete stays pending (the teardown waits for it again)
+  auto wait = [&](uint64_t* bar, uint32_t& ph, int& pend) {
+    if (!tc::mbar_wait_bounded(bar, ph, kT64WaitPolls)) {
+      timed_out = true;
+      tb.abort_ = 1;
+      return;
+    }
+    ph ^= 1u;
+    pend = 0;
+  };
+
+  // the previous tile's bra outputs -> FP64 -> its stored runs
+  auto bra_out = [&](uint32_t set, uint64_t base, uint32_t mkey) {
+    float sv[kTc64Orders][Q];
+    const uint32_t ta = tmem + tlane + set + c0;
+#pragma unroll
+    for (int o = 0; o < kTc64Orders; o++) tmem_ld_q<Q>(ta + o * R, sv[o]);
+    tc::tmem_wait_ld();
+    const int pa = (int)mkey + tb.ew[0][r] - 1106;
+    const int ebase = tb.lk[r] + lf_g;
+    uint64_t* arr = half ? im : re;
+#pragma unroll
+    for (int c = 0; c < Q; c++) {
+      const int bidx = cb + c;
+      const int64_t Y = combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c], sv[6][c], sv[7][c]);
+      const uint64_t bits = to_fp64(Y, pa + tb.ew[1][bidx]);
+      const int e = ebase + tb.lb[bidx];
+      const int run = e >> L;
+      if ((tb.stmask[run >> 5] >> (run & 31)) & 1) arr[base + tb.hioff[run] + (uint64_t)(e & (runlen - 1))] = bits;
+    }
+    tc::fence_before_sync();
+  };
+
+  const uint64_t t0 = blockIdx.x;
+  if (w == 0) {
+    if (t0 < ntiles) load_tile(t0, 0);
+    if (t0 + step < ntiles) load_tile(t0 + step, 1);
+  }
+  if (t0 < ntiles) pend_full[0] = 1;
+  if (t0 + step < ntiles) pend_full[1] = 1;
+
+  bool has_prev = false;
+  uint64_t prev_base = 0;
+  uint32_t prev_set = 0, prev_mkey = 0;
+  int it = 0;
+  for (uint64_t t = t0; t < ntiles; t += step, it++) {
+    const int b = it & 1;
+    const uint32_t set = (uint32_t)b * S::SET_COLS;
+    uint64_t* bre = bufs + (size_t)b * 2 * TILE;
+    uint64_t* bim = bre + TILE;
+    uint64_t* barr = half ? bim : bre;
+
+    // ---- 1, 2: ket digits of column (b = r, f)
+    wait(&tb.full[b], ph_full[b], pend_full[b]);
+    if (tid < 128) tb.brmax[b ^ 1][tid] = 0;  // the next tile's magnitude keys
+    uint32_t xl[Q], xh[Q];
+    uint32_t emx = 0;
+    {
+      const int e0 = tb.lb[r] + lf_g;
+#pragma unroll
+      for (int c = 0; c < Q; c++) {
+        const uint64_t v = barr[e0 + tb.lk[cb + c]];
+        xl[c] = (uint32_t)v;
+        xh[c] = (uint32_t)(v >> 32);
+        emx = max(emx, xh[c] & 0x7FF00000u);
+      }
+    }
+    tb.colmax[q][m] = emx;
+    __syncthreads();
+    if (tb.abort_) break;
+    uint32_t ecm = max(max(tb.colmax[0][m], tb.colmax[1][m]), max(tb.colmax[2][m], tb.colmax[3][m]));
+    ecm = max(ecm, 64u << 20);
+    const int Ec = (int)(ecm >> 20);
+    if (q == 0) tb.colE[m] = Ec;
+    {
+      float dg[Q][kTc64Slices];
+#pragma unroll
+      for (int c = 0; c < Q; c++) digits_fp64(xl[c], xh[c], ecm, dg[c]);
+      store_digits<K>(sAk, tc_kmajor_offset(m, c0, S::SBO), dg);
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+
+    // ---- 3: ket products
+    if (tid == 0) {
+      issue_step<K>(sAk, sB, tmem + set);
+      tc::mma_commit(&tb.mma[0]);
+    }
+    pend_mma[0] = 1;
+
+    // ---- 4: the previous tile's outputs
+    if (has_prev) {
+      wait(&tb.mma[1], ph_mma[1], pend_mma[1]);
+      tc::fence_after_sync();
+      if (!timed_out) bra_out(prev_set, prev_base, prev_mkey);
+    }
+
+    // ---- 5: ket outputs -> exact integers (in place of the tile), and the
+    // bra columns' magnitude keys: Ec + exponent of |S_0| + |S_1|/256 + 65,
+    // which bounds |Y| 2^Ec by 2^(key - 86) (1 + 2^-23)
+    wait(&tb.mma[0], ph_mma[0], pend_mma[0]);
+    tc::fence_after_sync();
+    if (!timed_out) {
+      float sv[kTc64Orders][Q];
+      const uint32_t ta = tmem + tlane + set + c0;
+#pragma unroll
+      for (int o = 0; o < kTc64Orders; o++) tmem_ld_q<Q>(ta + o * R, sv[o]);
+      tc::tmem_wait_ld();
+      const int e0 = tb.lb[r] + lf_g;
+#pragma unroll
+      for (int c = 0; c < Q; c++) {
+        const int a = cb + c;
+        barr[e0 + tb.lk[a]] =
+            (uint64_t)combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c], sv[6][c], sv[7][c]);
+        const float mag = fmaf(fabsf(sv[1][c]), 0.00390625f, fabsf(sv[0][c])) + 65.0f;
+        atomicMax(&tb.brmax[b][a * G + f], (uint32_t)Ec + (__float_as_uint(mag) >> 23));
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tb.abort_) break;
+    tc::fence_after_sync();
+
+    // ---- 6: bra digits of column (a = r, f): values Y_b 2^Ec(b) on the grid
+    // 2^(mkey - 141), |v| < 2^55 (1 + 2^-23)
+    const uint32_t mkey = tb.brmax[b][m];
+    {
+      float dg[Q][kTc64Slices];
+      const int e0 = tb.lk[r] + lf_g;
+#pragma unroll
+      for (int c = 0; c < Q; c++) {
+        const int bidx = cb + c;
+        const int64_t Y = (int64_t)barr[e0 + tb.lb[bidx]];
+        const int sh = (int)mkey - 141 - tb.colE[bidx * G + f];
+        const int64_t v = sh >= 0 ? shr_s64(Y, (uint32_t)sh) : shl_s64(Y, (uint32_t)(-sh));
+        digits_int(v, dg[c]);
+      }
+      store_digits<K>(sAb, tc_kmajor_offset(m, c0, S::SBO), dg);
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+
+    // ---- 7: bra products; 8: the loads two tiles ahead into this buffer
+    if (tid == 0) {
+      issue_step<K>(sAb, sB + kTc64Slices * S::B_BYTES, tmem + set);
+      tc::mma_commit(&tb.mma[1]);
+    }
+    pend_mma[1] = 1;
+    const uint64_t tn = t + 2 * step;
+    if (tn < ntiles) {
+      if (w == 0) load_tile(tn, b);
+      pend_full[b] = 1;
+    }
+    has_prev = true;
+    prev_base = tile_base(h, t);
+    prev_set = set;
+    prev_mkey = mkey;
+  }
+  if (has_prev && !tb.abort_) {
+    wait(&tb.mma[1], ph_mma[1], pend_mma[1]);
+    tc::fence_after_sync();
+    if (!timed_out) bra_out(prev_set, prev_base, prev_mkey);
+  }
+  // ---- teardown: nothing of this block may still be in flight when its
+  // tensor memory and shared memory are released (bounded, after an expiry)
+  __syncthreads();
+  const bool aborted = tb.abort_ != 0;
+  if (aborted) {
+    for (int i = 0; i < 2; i++) {
+      if (pend_mma[i]) tc::mbar_wait_bounded(&tb.mma[i], ph_mma[i], kT64WaitPolls << 2);
+      if (pend_full[i]) tc::mbar_wait_bounded(&tb.full[i], ph_full[i], kT64WaitPolls << 2);
+    }
+    if (tid == 0) atomicExch(err, 1);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (w == 0) tc::tmem_dealloc(tmem, S::TMEM_COLS);
+}
+
+template <int K>
+static cudaError_t configure_tc64() {
+  constexpr size_t smem = t64_smem_bytes<K>();
+  cudaError_t e = cudaFuncSetAttribute(k_pass_tc64<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_pass_tc64<K>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+  return e;
+}
+
+template <int K>
+static cudaError_t launch_tc64_k(const LaunchArgs& a, cudaStream_t s) {
+  static int configured = 0;
+  if (!configured) {
+    cudaError_t e = configure_tc64<K>();
+    if (e != cudaSuccess) return e;
+    configured = 1;
+  }
+  k_pass_tc64<K><<<a.grid, kT64Threads, t64_smem_bytes<K>(), s>>>(
+      static_cast<uint64_t*>(a.re), static_cast<uint64_t*>(a.im), static_cast<const TcDesc64<K>*>(a.desc), a.err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pass_tc64(const LaunchArgs& a, cudaStream_t s) {
+  if (!a.err || (a.K != 3 && a.K != 4) || a.arith != AR_FP64) return cudaErrorInvalidValue;
+  return a.K == 3 ? launch_tc64_k<3>(a, s) : launch_tc64_k<4>(a, s);
+}
+
+}  // namespace dmg

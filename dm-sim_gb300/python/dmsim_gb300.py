@@ -103,6 +103,7 @@ def lib():
         "dmsim_batch_autotune": [H, P(d)],
         "dmsim_append_channel": [H, u32, P(u32), u32, P(d)],
         "dmsim_append_noise": [H, ctypes.c_int, P(u32), d],
+        "dmsim_probe_rate": [ctypes.c_int, P(d)],
         "dmsim_plan_inspect": [u32, P(ctypes.c_int32), P(u32), P(d), P(d), u32, ctypes.c_int, ctypes.c_int,
                                ctypes.c_int, P(d), u32, P(u32)],
     }
@@ -480,6 +481,21 @@ def mlp_grad(params, X, T):
     loss = np.zeros(1, dtype=np.float32)
     _ok(lib().dmsim_mlp_grad(_fp(params), _fp(X), _fp(T), len(X), _fp(g), _fp(loss)), "mlp_grad")
     return g, float(loss[0])
+
+
+PROBES = ["fp64_fma", "fp32_fma", "dmma_flops", "int_lop3", "int_add", "int_shf", "int_prmt", "int_mad",
+          "cvt_s64_to_f64", "cvt_f32_f64", "cvt_f32_s32", "mix_fadd_lop3"]
+
+
+def probe_rates():
+    """Execution-unit throughputs of the current GPU (dmsim_probe_rate):
+    {probe name: operations per second}."""
+    out = {}
+    for i, name in enumerate(PROBES):
+        v = ctypes.c_double()
+        _ok(lib().dmsim_probe_rate(i, ctypes.byref(v)), "dmsim_probe_rate")
+        out[name] = v.value
+    return out
 
 
 class Batch:

@@ -27,7 +27,8 @@ enum dmsim_status {
   DMSIM_ERR_STATE = 2,        /* call out of order (upload twice, run before upload) */
   DMSIM_ERR_OOM = 3,          /* device or pinned host allocation failed */
   DMSIM_ERR_CUDA = 4,         /* CUDA runtime error (message in dmsim_last_error) */
-  DMSIM_ERR_TIMEOUT = 5,      /* a bounded device wait ran out */
+  DMSIM_ERR_TIMEOUT = 5,      /* a bounded device wait ran out; the run's results are undefined (a
+                                 single-circuit handle's rho must be reset or set before further use) */
   DMSIM_ERR_UNSUPPORTED = 6   /* e.g. n_gpus != 1: this engine is single-GPU */
 };
 
@@ -211,7 +212,8 @@ typedef struct dmsim_batch* dmsim_batch_handle;
 /* Batch-only options: the polls (128 ns naps) after which a work-queue
  * dependency wait gives up [2^25, ~4 s] -- the kernel then sets an error flag,
  * skips the item and finishes, and dmsim_batch_run returns
- * DMSIM_ERR_TIMEOUT -- and a test hook that makes the last pass of circuit 0
+ * DMSIM_ERR_TIMEOUT with every output of that run (diagonals, <ZZ>, states)
+ * set to NaN -- and a test hook that makes the last pass of circuit 0
  * wait for one tile more than its predecessor has, so that its waits run
  * out (failure detection without a GPU fault). */
 enum { DMSIM_BATCH_OPT_WAIT_LIMIT = 100, DMSIM_BATCH_OPT_TEST_STALL = 101 };
@@ -230,6 +232,27 @@ int dmsim_batch_get_dm(dmsim_batch_handle b, uint32_t circuit, double* re, doubl
 int dmsim_batch_autotune(dmsim_batch_handle b, double* best_ms);
 int dmsim_batch_stats(dmsim_batch_handle b, double out[8]);
 const char* dmsim_batch_last_error(dmsim_batch_handle b);
+/* ---- execution-unit throughput probes (no counterpart in the reference) ----
+ * The measurements behind the kernels' choice of arithmetic on this GPU: each
+ * probe runs fixed-length independent chains of one instruction kind on 8
+ * blocks of 256 threads per SM of the current device and returns operations
+ * per second (instructions, or FLOPs for the FP64 MMA). */
+enum dmsim_probe {
+  DMSIM_PROBE_FP64_FMA = 0,      /* fma.rn.f64 */
+  DMSIM_PROBE_FP32_FMA = 1,      /* fma.rn.f32 */
+  DMSIM_PROBE_DMMA = 2,          /* mma.sync m8n8k4 f64 (FP64 tensor core), FLOPs */
+  DMSIM_PROBE_INT_LOP3 = 3,      /* lop3.b32 */
+  DMSIM_PROBE_INT_ADD = 4,       /* add.u32 */
+  DMSIM_PROBE_INT_SHF = 5,       /* shf.r.clamp.b32 */
+  DMSIM_PROBE_INT_PRMT = 6,      /* prmt.b32 */
+  DMSIM_PROBE_INT_MAD = 7,       /* mad.lo.u32 */
+  DMSIM_PROBE_CVT_S64_F64 = 8,   /* cvt.rn.f64.s64 */
+  DMSIM_PROBE_CVT_F32_F64 = 9,   /* cvt.f64.f32 and cvt.rn.f32.f64, counted separately */
+  DMSIM_PROBE_CVT_F32_S32 = 10,  /* cvt.rni.s32.f32 and cvt.rn.f32.s32, counted separately */
+  DMSIM_PROBE_MIX_FADD_LOP3 = 11,/* add.rn.f32 and lop3.b32 interleaved, counted separately */
+  DMSIM_PROBE_COUNT = 12
+};
+int dmsim_probe_rate(int which, double* ops_per_s);
 /* Device pointers of rho (for in-HBM benchmarks and interop) */
 int dmsim_device_state(dmsim_handle h, void** re, void** im);
 const char* dmsim_last_error(dmsim_handle h);

@@ -62,6 +62,26 @@ def test_hea_sweep_shape(engine, oracle):
             assert np.abs(b.zz(c) - zz_from_diag(p, n)).max() <= 1e-9
 
 
+@pytest.mark.slow
+def test_hea_sweep_full_config(engine, oracle):
+    """The sweep at its full size: 512 hardware-efficient-ansatz circuits,
+    qubits uniform in {6..12}, 4-10 layers, in one persistent launch.  Every
+    circuit's diagonal and <Z_i Z_{i+1}> against the statevector oracle."""
+    sweep = W.hea_sweep(512, seed=4)
+    with engine.Batch([n for n, _ in sweep], mode="fused") as b:
+        for c, (n, circ) in enumerate(sweep):
+            b.extend(c, circ)
+        b.upload()
+        b.run()
+        worst_d = worst_z = 0.0
+        for c, (n, circ) in enumerate(sweep):
+            sr, si = oracle.sv_sim(n, circ)
+            p = sr ** 2 + si ** 2
+            worst_d = max(worst_d, float(np.abs(b.diag(c) - p).max()))
+            worst_z = max(worst_z, float(np.abs(b.zz(c) - zz_from_diag(p, n)).max()))
+    assert worst_d <= 1e-10 and worst_z <= 1e-9, (worst_d, worst_z)
+
+
 @pytest.mark.gpu
 def test_dependency_wait_runs_out_and_gpu_stays_usable(engine):
     """Failure detection without a GPU fault: a wait whose count never
@@ -76,6 +96,8 @@ def test_dependency_wait_runs_out_and_gpu_stays_usable(engine):
         with pytest.raises(engine.DMSimError) as e:
             b.run()
         assert e.value.status == engine.ERR_TIMEOUT
+        # no plausible-looking output survives an expired wait
+        assert np.isnan(b.diag(0)).all() and np.isnan(b.zz(1)).all()
     with engine.Batch([n for n, _ in sweep], mode="plain") as b:
         for c, (n, circ) in enumerate(sweep):
             b.extend(c, circ)

@@ -28,6 +28,28 @@ def test_table_mix_14q_fused_full_circuit(engine, oracle):
     assert abs(1 - m["fidelity"]) <= 1e-10 and abs(1 - m["trace"]) <= 1e-10, m
 
 
+@pytest.mark.parametrize("mode", ["plain", "fused"])
+def test_qft16_fp64_against_statevector(engine, oracle, mode):
+    """The 16-qubit FP64 workload (4^16 entries, 68.7 GB): a QFT ladder on an
+    X-Bernoulli(0.5) product input, then 1000 U3/CX layer gates.  The plain
+    gate-by-gate path (the reference's method) and the learned-fused path
+    against the statevector oracle: <= 1e-12 / 1e-10 max element error and
+    |1 - F| <= 1e-10."""
+    n = 16
+    circ = W.qft_then_layers(n, 1000, seed=3)
+    sr, si = oracle.sv_sim(n, circ)
+    psi = sr + 1j * si
+    kw = {"planner": "learned"} if mode == "fused" else {}
+    with engine.Simulation(n, mode=mode, **kw) as s:
+        s.extend(circ)
+        s.upload()
+        s.run()
+        m = s.pure_metrics(psi)
+    tol = 1e-12 if mode == "plain" else 1e-10
+    assert m["max_abs_err"] <= tol, m
+    assert abs(1 - m["fidelity"]) <= 1e-10 and abs(1 - m["trace"]) <= 1e-10, m
+
+
 def test_u3_cx_ccx_17q_complex64(engine, oracle):
     """17 qubits in complex64 (4^17 entries, 137 GB) against the FP64
     statevector oracle.  FP32 rounding leaves full-rank noise of Frobenius norm
