@@ -1,6 +1,7 @@
 // tensor64.cu -- dense K = 3, 4 qubit passes on the tensor cores for an FP64
-// state, at FP64 width, with no FP64 instruction (GB300's FP64 pipe and its
-// FP64 conversions run at ~1/60 of the FP32 rate).
+// state, at FP64 width, on the tensor cores and the integer/FP32 pipes:
+// GB300's FP64 pipe and its conversions run at ~1/60 of the FP32 rate, so it
+// does one conversion per output and nothing else.
 //
 // A pass is two products per tile, as in the double-float tensor pass: the
 // ket step multiplies every tile column x (2^K complex entries as R = 2^(K+1)
@@ -18,26 +19,30 @@
 // accumulator per order; every partial sum is an integer below 7 R 2^14 <=
 // 2^22, so the sums are exact.  The orders are combined in 64-bit integer
 // arithmetic (orders 6 and 7 below 2^-40 of order 0 enter through one
-// truncating shift) and the bra step's result is rounded once to FP64 (round
-// half up) from the 64-bit integer.  Error per step: below 2^-54 of the
-// column's largest value times the operator row's largest entry, per term;
-// FP64 dot products of the same length carry about 2^-53 per term.
+// truncating shift) and the bra step's result is rounded once to FP64 from
+// the 64-bit integer (one conversion per output on the FP64 pipe, which runs
+// beside the integer work).  Each value is held with 55 significant bits
+// relative to its column's largest (block floating point per column of 2^K
+// entries): the error of an output is below 2^-54 of its operator row's
+// 1-norm times its column's largest value, per step.
 //
-// Threads: 512 (16 warps), one block per SM.  Thread (warp w, lane l) owns
-// tile column m = 32 (w & 3) + l -- the TMEM lane its warp may read -- and
-// quarter q = w >> 2 of it: R/4 consecutive values (real parts for q < 2,
-// imaginary parts for q >= 2).  Per tile:
-//   1. wait for the tile (TMA bulk copies of its runs, issued two tiles ahead)
-//   2. ket digits -> A_ket;  3. one thread issues the ket MMAs (TMEM set t&1)
+// Threads: 16 arithmetic warps and one control warp, one block per SM.
+// Arithmetic thread (warp w, lane l) owns tile column m = 32 (w & 3) + l --
+// the TMEM lane its warp may read -- and quarter q = w >> 2 of it: R/4
+// consecutive values (real parts for q < 2, imaginary parts for q >= 2).
+// The control warp issues the MMAs (one lane) and the bulk copies.  Per tile:
+//   2. ket digits -> A_ket;  3. the ket MMAs (TMEM set t&1)
 //   4. the previous tile's bra accumulators -> FP64 -> global stores,
 //      overlapping the ket MMAs
 //   5. ket accumulators -> exact int64 outputs in the tile buffer
-//   6. bra digits -> A_bra;  7. one thread issues the bra MMAs (same set)
-//   8. warp 0 starts the loads of the tile two ahead into the freed buffer;
-//      the bra MMAs overlap the next tile's steps 1-3.
-// Every wait is bounded; on expiry the block sets the error flag, waits
-// (bounded) for its own copies and MMAs in flight, releases its TMEM and
-// returns, and the host reports DMSIM_ERR_TIMEOUT.
+//   6. bra digits -> A_bra; the next tile's values (TMA bulk copies of its
+//      runs, issued two tiles ahead) and their column maxima
+//   7. the bra MMAs (same set);  8. the loads two tiles ahead into the freed
+//      buffer.  The bra MMAs overlap the next tile's steps 2-3.
+// Three block barriers per tile (after steps 2, 5 and 6).  Every wait is
+// bounded; on expiry the block sets the error flag, waits (bounded) for its
+// own copies and MMAs in flight, releases its TMEM and returns, and the host
+// reports DMSIM_ERR_TIMEOUT.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -50,7 +55,7 @@ namespace dmg {
 
 namespace {
 
-constexpr int kT64Threads = 512;
+constexpr int kT64Threads = 512;  // arithmetic threads; one more warp issues the MMAs and copies
 constexpr uint32_t kT64WaitPolls = 1u << 24;
 
 template <int K>
@@ -77,7 +82,7 @@ struct T64Tables {
   int ew[2][D];
   uint32_t colmax[4][128];  // per quarter and column: largest FP64 exponent field
   uint32_t brmax[2][128];   // per tile parity and bra column: magnitude key of the ket outputs
-  int colE[128];            // biased exponent of each ket column's grid
+  int colEt[128 / D][D];    // biased exponent of ket column (b, f)'s grid, at [f][b]
   uint32_t slot;
   int abort_;
 };
@@ -161,42 +166,25 @@ __device__ __forceinline__ int64_t combine_orders(float s0, float s1, float s2, 
   return ((int64_t)p01 << 32) + ((int64_t)p23 << 16) + (int64_t)(p45 + p67);
 }
 
-// The FP64 bits of Y 2^P, rounded half up to 53 bits; 0 for Y = 0 or below
-// the normal range.
+// The FP64 bits of Y 2^P: one conversion on the FP64 pipe (correctly
+// rounded), then P added to the exponent field.  0 for Y = 0 and below the
+// normal range.
 __device__ __forceinline__ uint64_t to_fp64(int64_t Y, int P) {
-  const uint64_t s = (uint64_t)(Y >> 63);
-  const uint64_t a = ((uint64_t)Y ^ s) - s;
-  const int lz = __clzll((long long)a);
-  const uint64_t nrm = a << (lz & 63);
-  const uint64_t mant = (nrm >> 11) + ((nrm >> 10) & 1);  // 2^52 <= mant <= 2^53
-  const int E = 1086 - lz + P;                            // biased exponent of the value
-  const uint64_t bits = ((uint64_t)(E - 1) << 52) + mant + (s << 63);
-  return (a == 0 || E <= 0) ? 0ull : bits;
+  const uint64_t b = (uint64_t)__double_as_longlong(__ll2double_rn((long long)Y));
+  const int E = (int)((b >> 52) & 0x7FF) + P;
+  return (Y != 0 && E > 0) ? b + ((uint64_t)(int64_t)P << 52) : 0ull;
 }
 
-template <int Q>
-__device__ __forceinline__ void tmem_ld_q(uint32_t taddr, float (&v)[Q]) {
-  if constexpr (Q == 8) tc::tmem_ld8(taddr, v);
-  else tc::tmem_ld4(taddr, v);
-}
-
-// Pack Q digits of slice j (Q consecutive K indices of row m) into the
-// K-major operand: 16 bytes (Q = 8) or 8 bytes (Q = 4).
-template <int K>
-__device__ __forceinline__ void store_digits(unsigned char* sA, uint32_t off, const float (&dg)[T64<K>::Q][kTc64Slices]) {
-  using S = T64<K>;
+// Pack the digits of 4 consecutive K indices of row m into the K-major
+// operand, 8 bytes per slice.
+__device__ __forceinline__ void store_digits4(unsigned char* sA, uint32_t a_bytes, uint32_t off,
+                                              const float (&dg)[4][kTc64Slices]) {
 #pragma unroll
   for (int j = 0; j < kTc64Slices; j++) {
-    uint32_t pk[S::Q / 2];
-#pragma unroll
-    for (int c = 0; c < S::Q; c += 2) {
-      const __nv_bfloat162 v = __floats2bfloat162_rn(dg[c][j], dg[c + 1][j]);  // exact: |digit| <= 128
-      pk[c >> 1] = *reinterpret_cast<const uint32_t*>(&v);
-    }
-    if constexpr (S::Q == 8)
-      *reinterpret_cast<uint4*>(sA + j * S::A_BYTES + off) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-    else
-      *reinterpret_cast<uint2*>(sA + j * S::A_BYTES + off) = make_uint2(pk[0], pk[1]);
+    const __nv_bfloat162 v0 = __floats2bfloat162_rn(dg[0][j], dg[1][j]);  // exact: |digit| <= 128
+    const __nv_bfloat162 v1 = __floats2bfloat162_rn(dg[2][j], dg[3][j]);
+    *reinterpret_cast<uint2*>(sA + j * a_bytes + off) =
+        make_uint2(*reinterpret_cast<const uint32_t*>(&v0), *reinterpret_cast<const uint32_t*>(&v1));
   }
 }
 
@@ -228,7 +216,7 @@ __device__ __forceinline__ void issue_step(const unsigned char* sA, const unsign
 }  // namespace
 
 template <int K>
-__global__ void __launch_bounds__(kT64Threads, 1)
+__global__ void __launch_bounds__(kT64Threads + 32, 1)
     k_pass_tc64(uint64_t* __restrict__ re, uint64_t* __restrict__ im, const TcDesc64<K>* __restrict__ dp,
                 int* __restrict__ err) {
   using S = T64<K>;
@@ -241,7 +229,8 @@ __global__ void __launch_bounds__(kT64Threads, 1)
   T64Tables<K>& tb = *reinterpret_cast<T64Tables<K>*>(bufs + 4 * TILE);
   const PassHeader& h = dp->h;
   const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
-  const int m = 32 * (w & 3) + l, q = w >> 2;
+  const bool ctl = w == kT64Threads / 32;  // the control warp: MMA and copy issue only
+  const int m = 32 * (w & 3) + l, q = (w >> 2) & 3;
   const int r = m / G, f = m & (G - 1);
   const int c0 = q * Q;       // first value of this thread's quarter of a column
   const int half = c0 / D;    // 0: real parts, 1: imaginary parts
@@ -294,28 +283,39 @@ __global__ void __launch_bounds__(kT64Threads, 1)
 
   int lf_g = 0;  // free-bit offset of this column's group f (the same in both steps)
   for (int j = 0; j < h.g; j++) lf_g |= ((f >> j) & 1) << h.freepos[j];
-  const int L = h.L, runlen = 1 << L, nruns = 1 << h.mhi;
+  const int L = h.L, runlen = 1 << L, ncopies = 2 << h.mhi;  // runs of the real and imaginary arrays
   const uint64_t ntiles = h.ntiles, step = gridDim.x;
+  // this thread's values of the loaded tile (ket step): entries (a = cb + c, r, f) at basek + offk[c]
+  int offk[Q];
+#pragma unroll
+  for (int c = 0; c < Q; c++) offk[c] = tb.lk[cb + c];
+  const int basek = tb.lb[r] + lf_g;
+  // Accumulators are read and digits written 4 values at a time: 17 warps
+  // leave 96 registers per thread.
+  constexpr int QH = 4;
+  // The ket step's exact integer outputs replace the tile in its buffer, at
+  // [half][a][b ^ (a & 1)][f]: the ket step writes, for one a, 32 consecutive
+  // words per warp, and the bra step reads, for one b, columns a of both
+  // parities -- both free of bank conflicts.
+  auto yidx = [&](int a, int b) { return half * TILE + (a * D + (b ^ (a & 1))) * G + f; };
 
-  // warp 0: every run of tile t (real and imaginary arrays) into buffer b
+  // control warp: the loads of tile t into buffer b, the buffer's barrier
+  // armed with the tile's bytes first; one 1-D bulk copy per run and array
   auto load_tile = [&](uint64_t t, int b) {
     uint64_t* dst = bufs + (size_t)b * 2 * TILE;
     const uint64_t base = tile_base(h, t);
-    if (l == 0) {
-      tc::fence_proxy_async_smem();
-      tc::mbar_arrive_expect_tx(&tb.full[b], S::BUF_BYTES);
-    }
+    if (l == 0) tc::mbar_arrive_expect_tx(&tb.full[b], S::BUF_BYTES);
     __syncwarp();
-    for (int i = l; i < 2 * nruns; i += 32) {
+    for (int i = l; i < ncopies; i += 32) {
       const int run = i >> 1, arr = i & 1;
-      const uint64_t* src = (arr ? im : re) + base + tb.hioff[run];
-      tc::bulk_g2s(dst + arr * TILE + run * runlen, src, (uint32_t)runlen * 8u, &tb.full[b]);
+      tc::bulk_g2s(dst + arr * TILE + run * runlen, (arr ? im : re) + base + tb.hioff[run], (uint32_t)runlen * 8u,
+                   &tb.full[b]);
     }
   };
 
-  // outstanding asynchronous work, the same on every thread
-  uint32_t ph_full[2] = {0, 0}, ph_mma[2] = {0, 0};
-  int pend_full[2] = {0, 0}, pend_mma[2] = {0, 0};
+  // outstanding asynchronous work, tracked by the arithmetic warps
+  uint32_t phf0 = 0, phf1 = 0, phk = 0, phb = 0;
+  int pendf0 = 0, pendf1 = 0, pendk = 0, pendb = 0;
   bool timed_out = false;
   // a phase that did not complete stays pending (the teardown waits for it again)
   auto wait = [&](uint64_t* bar, uint32_t& ph, int& pend) {
@@ -327,114 +327,134 @@ __global__ void __launch_bounds__(kT64Threads, 1)
     ph ^= 1u;
     pend = 0;
   };
+  auto wait_full = [&](int b) {
+    if (b) wait(&tb.full[1], phf1, pendf1);
+    else wait(&tb.full[0], phf0, pendf0);
+  };
 
   // the previous tile's bra outputs -> FP64 -> its stored runs
   auto bra_out = [&](uint32_t set, uint64_t base, uint32_t mkey) {
-    float sv[kTc64Orders][Q];
-    const uint32_t ta = tmem + tlane + set + c0;
-#pragma unroll
-    for (int o = 0; o < kTc64Orders; o++) tmem_ld_q<Q>(ta + o * R, sv[o]);
-    tc::tmem_wait_ld();
     const int pa = (int)mkey + tb.ew[0][r] - 1106;
-    const int ebase = tb.lk[r] + lf_g;
+    const int baseb = tb.lk[r] + lf_g;
     uint64_t* arr = half ? im : re;
 #pragma unroll
-    for (int c = 0; c < Q; c++) {
-      const int bidx = cb + c;
-      const int64_t Y = combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c], sv[6][c], sv[7][c]);
-      const uint64_t bits = to_fp64(Y, pa + tb.ew[1][bidx]);
-      const int e = ebase + tb.lb[bidx];
-      const int run = e >> L;
-      if ((tb.stmask[run >> 5] >> (run & 31)) & 1) arr[base + tb.hioff[run] + (uint64_t)(e & (runlen - 1))] = bits;
+    for (int c4 = 0; c4 < Q; c4 += QH) {
+      float sv[kTc64Orders][QH];
+      const uint32_t ta = tmem + tlane + set + c0 + c4;
+#pragma unroll
+      for (int o = 0; o < kTc64Orders; o++) tc::tmem_ld4(ta + o * R, sv[o]);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int c = 0; c < QH; c++) {
+        const int64_t Y =
+            combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c], sv[6][c], sv[7][c]);
+        const uint64_t bits = to_fp64(Y, pa + tb.ew[1][cb + c4 + c]);
+        const int e = baseb + tb.lb[cb + c4 + c];
+        const int run = e >> L;
+        if ((tb.stmask[run >> 5] >> (run & 31)) & 1) arr[base + tb.hioff[run] + (uint64_t)(e & (runlen - 1))] = bits;
+      }
     }
     tc::fence_before_sync();
   };
 
+  // this thread's values of the tile in buffer b (ket step) and their largest exponent field
+  uint32_t xl[Q], xh[Q];
+  auto read_tile = [&](int b) {
+    const uint64_t* barr = bufs + (size_t)b * 2 * TILE + (half ? TILE : 0);
+    uint32_t emx = 0;
+#pragma unroll
+    for (int c = 0; c < Q; c++) {
+      const uint64_t v = barr[basek + offk[c]];
+      xl[c] = (uint32_t)v;
+      xh[c] = (uint32_t)(v >> 32);
+      emx = max(emx, xh[c] & 0x7FF00000u);
+    }
+    tb.colmax[q][m] = emx;
+  };
+
+  // ---- prologue: the first two tiles in flight, the first one's values
   const uint64_t t0 = blockIdx.x;
-  if (w == 0) {
+  if (ctl) {
     if (t0 < ntiles) load_tile(t0, 0);
     if (t0 + step < ntiles) load_tile(t0 + step, 1);
+  } else {
+    pendf0 = t0 < ntiles;
+    pendf1 = t0 + step < ntiles;
+    if (t0 < ntiles) {
+      wait_full(0);
+      read_tile(0);
+    }
   }
-  if (t0 < ntiles) pend_full[0] = 1;
-  if (t0 + step < ntiles) pend_full[1] = 1;
+  __syncthreads();
 
   bool has_prev = false;
   uint64_t prev_base = 0;
   uint32_t prev_set = 0, prev_mkey = 0;
   int it = 0;
   for (uint64_t t = t0; t < ntiles; t += step, it++) {
+    if (tb.abort_) break;
     const int b = it & 1;
     const uint32_t set = (uint32_t)b * S::SET_COLS;
-    uint64_t* bre = bufs + (size_t)b * 2 * TILE;
-    uint64_t* bim = bre + TILE;
-    uint64_t* barr = half ? bim : bre;
+    uint64_t* buf = bufs + (size_t)b * 2 * TILE;
+    const uint64_t tn = t + 2 * step;
 
-    // ---- 1, 2: ket digits of column (b = r, f)
-    wait(&tb.full[b], ph_full[b], pend_full[b]);
-    if (tid < 128) tb.brmax[b ^ 1][tid] = 0;  // the next tile's magnitude keys
-    uint32_t xl[Q], xh[Q];
-    uint32_t emx = 0;
-    {
-      const int e0 = tb.lb[r] + lf_g;
+    // ---- 2: ket digits of column (b = r, f), from the values read before the last barrier
+    int Ec = 0;
+    if (!ctl) {
+      uint32_t ecm = max(max(tb.colmax[0][m], tb.colmax[1][m]), max(tb.colmax[2][m], tb.colmax[3][m]));
+      ecm = max(ecm, 64u << 20);
+      Ec = (int)(ecm >> 20);
+      if (q == 0) tb.colEt[f][r] = Ec;
 #pragma unroll
-      for (int c = 0; c < Q; c++) {
-        const uint64_t v = barr[e0 + tb.lk[cb + c]];
-        xl[c] = (uint32_t)v;
-        xh[c] = (uint32_t)(v >> 32);
-        emx = max(emx, xh[c] & 0x7FF00000u);
+      for (int c4 = 0; c4 < Q; c4 += QH) {
+        float dg[QH][kTc64Slices];
+#pragma unroll
+        for (int c = 0; c < QH; c++) digits_fp64(xl[c4 + c], xh[c4 + c], ecm, dg[c]);
+        store_digits4(sAk, S::A_BYTES, tc_kmajor_offset(m, c0 + c4, S::SBO), dg);
       }
+      tc::fence_proxy_async_smem();
     }
-    tb.colmax[q][m] = emx;
-    __syncthreads();
-    if (tb.abort_) break;
-    uint32_t ecm = max(max(tb.colmax[0][m], tb.colmax[1][m]), max(tb.colmax[2][m], tb.colmax[3][m]));
-    ecm = max(ecm, 64u << 20);
-    const int Ec = (int)(ecm >> 20);
-    if (q == 0) tb.colE[m] = Ec;
-    {
-      float dg[Q][kTc64Slices];
-#pragma unroll
-      for (int c = 0; c < Q; c++) digits_fp64(xl[c], xh[c], ecm, dg[c]);
-      store_digits<K>(sAk, tc_kmajor_offset(m, c0, S::SBO), dg);
-    }
-    tc::fence_proxy_async_smem();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
 
     // ---- 3: ket products
-    if (tid == 0) {
-      issue_step<K>(sAk, sB, tmem + set);
-      tc::mma_commit(&tb.mma[0]);
-    }
-    pend_mma[0] = 1;
-
-    // ---- 4: the previous tile's outputs
-    if (has_prev) {
-      wait(&tb.mma[1], ph_mma[1], pend_mma[1]);
+    if (ctl) {
+      if (l == 0) {
+        issue_step<K>(sAk, sB, tmem + set);
+        tc::mma_commit(&tb.mma[0]);
+      }
+      __syncwarp();
+    } else {
+      pendk = 1;
+      // ---- 4: the previous tile's outputs (overlapping the ket products)
+      if (has_prev) {
+        wait(&tb.mma[1], phb, pendb);
+        tc::fence_after_sync();
+        if (!timed_out) bra_out(prev_set, prev_base, prev_mkey);
+      }
+      // ---- 5: ket outputs -> exact integers (in place of the tile), and the
+      // bra columns' magnitude keys: Ec + exponent of |S_0| + |S_1|/256 + 65,
+      // which bounds |Y| 2^Ec by 2^(key - 86) (1 + 2^-23)
+      wait(&tb.mma[0], phk, pendk);
       tc::fence_after_sync();
-      if (!timed_out) bra_out(prev_set, prev_base, prev_mkey);
-    }
-
-    // ---- 5: ket outputs -> exact integers (in place of the tile), and the
-    // bra columns' magnitude keys: Ec + exponent of |S_0| + |S_1|/256 + 65,
-    // which bounds |Y| 2^Ec by 2^(key - 86) (1 + 2^-23)
-    wait(&tb.mma[0], ph_mma[0], pend_mma[0]);
-    tc::fence_after_sync();
-    if (!timed_out) {
-      float sv[kTc64Orders][Q];
-      const uint32_t ta = tmem + tlane + set + c0;
+      if (!timed_out) {
 #pragma unroll
-      for (int o = 0; o < kTc64Orders; o++) tmem_ld_q<Q>(ta + o * R, sv[o]);
-      tc::tmem_wait_ld();
-      const int e0 = tb.lb[r] + lf_g;
+        for (int c4 = 0; c4 < Q; c4 += QH) {
+          float sv[kTc64Orders][QH];
+          const uint32_t ta = tmem + tlane + set + c0 + c4;
 #pragma unroll
-      for (int c = 0; c < Q; c++) {
-        const int a = cb + c;
-        barr[e0 + tb.lk[a]] =
-            (uint64_t)combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c], sv[6][c], sv[7][c]);
-        const float mag = fmaf(fabsf(sv[1][c]), 0.00390625f, fabsf(sv[0][c])) + 65.0f;
-        atomicMax(&tb.brmax[b][a * G + f], (uint32_t)Ec + (__float_as_uint(mag) >> 23));
+          for (int o = 0; o < kTc64Orders; o++) tc::tmem_ld4(ta + o * R, sv[o]);
+          tc::tmem_wait_ld();
+#pragma unroll
+          for (int c = 0; c < QH; c++) {
+            const int a = cb + c4 + c;
+            buf[yidx(a, r)] = (uint64_t)combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c],
+                                                       sv[6][c], sv[7][c]);
+            const float mag = fmaf(fabsf(sv[1][c]), 0.00390625f, fabsf(sv[0][c])) + 65.0f;
+            atomicMax(&tb.brmax[b][a * G + f], (uint32_t)Ec + (__float_as_uint(mag) >> 23));
+          }
+        }
       }
     }
     tc::fence_before_sync();
@@ -444,55 +464,68 @@ __global__ void __launch_bounds__(kT64Threads, 1)
 
     // ---- 6: bra digits of column (a = r, f): values Y_b 2^Ec(b) on the grid
     // 2^(mkey - 141), |v| < 2^55 (1 + 2^-23)
-    const uint32_t mkey = tb.brmax[b][m];
-    {
-      float dg[Q][kTc64Slices];
-      const int e0 = tb.lk[r] + lf_g;
+    const uint32_t mkey = ctl ? 0u : tb.brmax[b][m];
+    if (!ctl) {
+      int ecol[Q];
 #pragma unroll
-      for (int c = 0; c < Q; c++) {
-        const int bidx = cb + c;
-        const int64_t Y = (int64_t)barr[e0 + tb.lb[bidx]];
-        const int sh = (int)mkey - 141 - tb.colE[bidx * G + f];
-        const int64_t v = sh >= 0 ? shr_s64(Y, (uint32_t)sh) : shl_s64(Y, (uint32_t)(-sh));
-        digits_int(v, dg[c]);
+      for (int c = 0; c < Q; c++) ecol[c] = tb.colEt[f][cb + c];
+#pragma unroll
+      for (int c4 = 0; c4 < Q; c4 += QH) {
+        float dg[QH][kTc64Slices];
+#pragma unroll
+        for (int c = 0; c < QH; c++) {
+          const int64_t Y = (int64_t)buf[yidx(r, cb + c4 + c)];
+          const int sh = (int)mkey - 141 - ecol[c4 + c];
+          const int64_t v = sh >= 0 ? shr_s64(Y, (uint32_t)sh) : shl_s64(Y, (uint32_t)(-sh));
+          digits_int(v, dg[c]);
+        }
+        store_digits4(sAb, S::A_BYTES, tc_kmajor_offset(m, c0 + c4, S::SBO), dg);
       }
-      store_digits<K>(sAb, tc_kmajor_offset(m, c0, S::SBO), dg);
+      // the next tile's values (its loads were issued two tiles ago)
+      if (t + step < ntiles) {
+        wait_full(b ^ 1);
+        read_tile(b ^ 1);
+      }
+      if (tid < 128) tb.brmax[b ^ 1][tid] = 0;  // the next tile's magnitude keys
+      tc::fence_proxy_async_smem();
     }
-    tc::fence_proxy_async_smem();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
 
     // ---- 7: bra products; 8: the loads two tiles ahead into this buffer
-    if (tid == 0) {
-      issue_step<K>(sAb, sB + kTc64Slices * S::B_BYTES, tmem + set);
-      tc::mma_commit(&tb.mma[1]);
-    }
-    pend_mma[1] = 1;
-    const uint64_t tn = t + 2 * step;
-    if (tn < ntiles) {
-      if (w == 0) load_tile(tn, b);
-      pend_full[b] = 1;
+    if (ctl) {
+      if (l == 0) {
+        issue_step<K>(sAb, sB + kTc64Slices * S::B_BYTES, tmem + set);
+        tc::mma_commit(&tb.mma[1]);
+      }
+      __syncwarp();
+      if (tn < ntiles) load_tile(tn, b);
+    } else {
+      pendb = 1;
+      if (tn < ntiles) {
+        if (b) pendf1 = 1;
+        else pendf0 = 1;
+      }
     }
     has_prev = true;
     prev_base = tile_base(h, t);
     prev_set = set;
     prev_mkey = mkey;
   }
-  if (has_prev && !tb.abort_) {
-    wait(&tb.mma[1], ph_mma[1], pend_mma[1]);
+  if (!ctl && has_prev && !tb.abort_) {
+    wait(&tb.mma[1], phb, pendb);
     tc::fence_after_sync();
     if (!timed_out) bra_out(prev_set, prev_base, prev_mkey);
   }
   // ---- teardown: nothing of this block may still be in flight when its
   // tensor memory and shared memory are released (bounded, after an expiry)
   __syncthreads();
-  const bool aborted = tb.abort_ != 0;
-  if (aborted) {
-    for (int i = 0; i < 2; i++) {
-      if (pend_mma[i]) tc::mbar_wait_bounded(&tb.mma[i], ph_mma[i], kT64WaitPolls << 2);
-      if (pend_full[i]) tc::mbar_wait_bounded(&tb.full[i], ph_full[i], kT64WaitPolls << 2);
-    }
+  if (tb.abort_ && !ctl) {
+    if (pendk) tc::mbar_wait_bounded(&tb.mma[0], phk, kT64WaitPolls << 2);
+    if (pendb) tc::mbar_wait_bounded(&tb.mma[1], phb, kT64WaitPolls << 2);
+    if (pendf0) tc::mbar_wait_bounded(&tb.full[0], phf0, kT64WaitPolls << 2);
+    if (pendf1) tc::mbar_wait_bounded(&tb.full[1], phf1, kT64WaitPolls << 2);
     if (tid == 0) atomicExch(err, 1);
   }
   tc::fence_before_sync();
@@ -519,7 +552,7 @@ static cudaError_t launch_tc64_k(const LaunchArgs& a, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     configured = 1;
   }
-  k_pass_tc64<K><<<a.grid, kT64Threads, t64_smem_bytes<K>(), s>>>(
+  k_pass_tc64<K><<<a.grid, kT64Threads + 32, t64_smem_bytes<K>(), s>>>(
       static_cast<uint64_t*>(a.re), static_cast<uint64_t*>(a.im), static_cast<const TcDesc64<K>*>(a.desc), a.err);
   return cudaGetLastError();
 }

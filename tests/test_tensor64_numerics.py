@@ -3,7 +3,7 @@ bit for bit on the CPU with Python integers: FP64 bits aligned to a column
 grid, 7 balanced base-256 digits, exact order sums (checked below 2^22, the
 bound the kernel's integer extraction needs), 64-bit combination of the
 orders, the bra columns' magnitude keys and alignment, and the final rounding
-to FP64.  Checked against exact rational arithmetic on random unitaries and
+to FP64 (one correctly rounded conversion).  Checked against exact rational arithmetic on random unitaries and
 density-matrix blocks with columns of very different sizes (bounds in the
 test's docstring)."""
 import struct
@@ -99,17 +99,14 @@ def key(s, ec):
 
 
 def to_fp64(y, p):
+    """tensor64.cu to_fp64: the correctly rounded double of y, times 2^p."""
     if y == 0:
         return 0.0
-    a = abs(y)
-    lz = 64 - a.bit_length()
-    nrm = a << lz
-    mant = (nrm >> 11) + ((nrm >> 10) & 1)
-    e = 1086 - lz + p
+    d = float(y)  # round to nearest even, as cvt.rn.f64.s64
+    e = ((f64_bits(d) >> 52) & 0x7FF) + p
     if e <= 0:
         return 0.0
-    bits = ((e - 1) << 52) + mant + ((1 << 63) if y < 0 else 0)
-    return bits_f64(bits)
+    return bits_f64(f64_bits(d) + (p << 52))
 
 
 def real_embedding(m):
