@@ -26,11 +26,11 @@
 // entries): the error of an output is below 2^-54 of its operator row's
 // 1-norm times its column's largest value, per step.
 //
-// Threads: 16 arithmetic warps and one control warp, one block per SM.
-// Arithmetic thread (warp w, lane l) owns tile column m = 32 (w & 3) + l --
-// the TMEM lane its warp may read -- and quarter q = w >> 2 of it: R/4
-// consecutive values (real parts for q < 2, imaginary parts for q >= 2).
-// The control warp issues the MMAs (one lane) and the bulk copies.  Per tile:
+// Threads: 512 (16 warps), one block per SM.  Thread (warp w, lane l) owns
+// tile column m = 32 (w & 3) + l -- the TMEM lane its warp may read -- and
+// quarter q = w >> 2 of it: R/4 consecutive values (real parts for q < 2,
+// imaginary parts for q >= 2).  Thread 0 issues the MMAs; every thread
+// issues its share of the bulk copies.  Per tile:
 //   2. ket digits -> A_ket;  3. the ket MMAs (TMEM set t&1)
 //   4. the previous tile's bra accumulators -> FP64 -> global stores,
 //      overlapping the ket MMAs
@@ -55,7 +55,7 @@ namespace dmg {
 
 namespace {
 
-constexpr int kT64Threads = 512;  // arithmetic threads; one more warp issues the MMAs and copies
+constexpr int kT64Threads = 512;
 constexpr uint32_t kT64WaitPolls = 1u << 24;
 
 template <int K>
@@ -216,7 +216,7 @@ __device__ __forceinline__ void issue_step(const unsigned char* sA, const unsign
 }  // namespace
 
 template <int K>
-__global__ void __launch_bounds__(kT64Threads + 32, 1)
+__global__ void __launch_bounds__(kT64Threads, 1)
     k_pass_tc64(uint64_t* __restrict__ re, uint64_t* __restrict__ im, const TcDesc64<K>* __restrict__ dp,
                 int* __restrict__ err) {
   using S = T64<K>;
@@ -229,8 +229,7 @@ __global__ void __launch_bounds__(kT64Threads + 32, 1)
   T64Tables<K>& tb = *reinterpret_cast<T64Tables<K>*>(bufs + 4 * TILE);
   const PassHeader& h = dp->h;
   const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
-  const bool ctl = w == kT64Threads / 32;  // the control warp: MMA and copy issue only
-  const int m = 32 * (w & 3) + l, q = (w >> 2) & 3;
+  const int m = 32 * (w & 3) + l, q = w >> 2;
   const int r = m / G, f = m & (G - 1);
   const int c0 = q * Q;       // first value of this thread's quarter of a column
   const int half = c0 / D;    // 0: real parts, 1: imaginary parts
@@ -290,8 +289,7 @@ __global__ void __launch_bounds__(kT64Threads + 32, 1)
 #pragma unroll
   for (int c = 0; c < Q; c++) offk[c] = tb.lk[cb + c];
   const int basek = tb.lb[r] + lf_g;
-  // Accumulators are read and digits written 4 values at a time: 17 warps
-  // leave 96 registers per thread.
+  // accumulators are read and digits written 4 values at a time
   constexpr int QH = 4;
   // The ket step's exact integer outputs replace the tile in its buffer, at
   // [half][a][b ^ (a & 1)][f]: the ket step writes, for one a, 32 consecutive
@@ -299,21 +297,20 @@ __global__ void __launch_bounds__(kT64Threads + 32, 1)
   // parities -- both free of bank conflicts.
   auto yidx = [&](int a, int b) { return half * TILE + (a * D + (b ^ (a & 1))) * G + f; };
 
-  // control warp: the loads of tile t into buffer b, the buffer's barrier
-  // armed with the tile's bytes first; one 1-D bulk copy per run and array
-  auto load_tile = [&](uint64_t t, int b) {
+  // Loads of a tile: thread 0 arms the buffer's barrier with the tile's bytes
+  // before a block barrier, after which every thread issues its share of the
+  // 1-D bulk copies (one per run of each array).
+  auto copy_tile = [&](uint64_t t, int b) {
     uint64_t* dst = bufs + (size_t)b * 2 * TILE;
     const uint64_t base = tile_base(h, t);
-    if (l == 0) tc::mbar_arrive_expect_tx(&tb.full[b], S::BUF_BYTES);
-    __syncwarp();
-    for (int i = l; i < ncopies; i += 32) {
+    for (int i = tid; i < ncopies; i += kT64Threads) {
       const int run = i >> 1, arr = i & 1;
       tc::bulk_g2s(dst + arr * TILE + run * runlen, (arr ? im : re) + base + tb.hioff[run], (uint32_t)runlen * 8u,
                    &tb.full[b]);
     }
   };
 
-  // outstanding asynchronous work, tracked by the arithmetic warps
+  // outstanding asynchronous work, the same on every thread
   uint32_t phf0 = 0, phf1 = 0, phk = 0, phb = 0;
   int pendf0 = 0, pendf1 = 0, pendk = 0, pendb = 0;
   bool timed_out = false;
@@ -374,16 +371,18 @@ __global__ void __launch_bounds__(kT64Threads + 32, 1)
 
   // ---- prologue: the first two tiles in flight, the first one's values
   const uint64_t t0 = blockIdx.x;
-  if (ctl) {
-    if (t0 < ntiles) load_tile(t0, 0);
-    if (t0 + step < ntiles) load_tile(t0 + step, 1);
-  } else {
-    pendf0 = t0 < ntiles;
-    pendf1 = t0 + step < ntiles;
-    if (t0 < ntiles) {
-      wait_full(0);
-      read_tile(0);
-    }
+  if (tid == 0) {
+    if (t0 < ntiles) tc::mbar_arrive_expect_tx(&tb.full[0], S::BUF_BYTES);
+    if (t0 + step < ntiles) tc::mbar_arrive_expect_tx(&tb.full[1], S::BUF_BYTES);
+  }
+  __syncthreads();
+  if (t0 < ntiles) copy_tile(t0, 0);
+  if (t0 + step < ntiles) copy_tile(t0 + step, 1);
+  pendf0 = t0 < ntiles;
+  pendf1 = t0 + step < ntiles;
+  if (t0 < ntiles) {
+    wait_full(0);
+    read_tile(0);
   }
   __syncthreads();
 
@@ -400,7 +399,7 @@ __global__ void __launch_bounds__(kT64Threads + 32, 1)
 
     // ---- 2: ket digits of column (b = r, f), from the values read before the last barrier
     int Ec = 0;
-    if (!ctl) {
+    {
       uint32_t ecm = max(max(tb.colmax[0][m], tb.colmax[1][m]), max(tb.colmax[2][m], tb.colmax[3][m]));
       ecm = max(ecm, 64u << 20);
       Ec = (int)(ecm >> 20);
@@ -419,13 +418,11 @@ __global__ void __launch_bounds__(kT64Threads + 32, 1)
     tc::fence_after_sync();
 
     // ---- 3: ket products
-    if (ctl) {
-      if (l == 0) {
-        issue_step<K>(sAk, sB, tmem + set);
-        tc::mma_commit(&tb.mma[0]);
-      }
-      __syncwarp();
-    } else {
+    if (tid == 0) {
+      issue_step<K>(sAk, sB, tmem + set);
+      tc::mma_commit(&tb.mma[0]);
+    }
+    {
       pendk = 1;
       // ---- 4: the previous tile's outputs (overlapping the ket products)
       if (has_prev) {
@@ -464,8 +461,8 @@ __global__ void __launch_bounds__(kT64Threads + 32, 1)
 
     // ---- 6: bra digits of column (a = r, f): values Y_b 2^Ec(b) on the grid
     // 2^(mkey - 141), |v| < 2^55 (1 + 2^-23)
-    const uint32_t mkey = ctl ? 0u : tb.brmax[b][m];
-    if (!ctl) {
+    const uint32_t mkey = tb.brmax[b][m];
+    {
       int ecol[Q];
 #pragma unroll
       for (int c = 0; c < Q; c++) ecol[c] = tb.colEt[f][cb + c];
@@ -487,6 +484,7 @@ __global__ void __launch_bounds__(kT64Threads + 32, 1)
         read_tile(b ^ 1);
       }
       if (tid < 128) tb.brmax[b ^ 1][tid] = 0;  // the next tile's magnitude keys
+      if (tid == 0 && tn < ntiles) tc::mbar_arrive_expect_tx(&tb.full[b], S::BUF_BYTES);  // this buffer's next loads
       tc::fence_proxy_async_smem();
     }
     tc::fence_before_sync();
@@ -494,26 +492,22 @@ __global__ void __launch_bounds__(kT64Threads + 32, 1)
     tc::fence_after_sync();
 
     // ---- 7: bra products; 8: the loads two tiles ahead into this buffer
-    if (ctl) {
-      if (l == 0) {
-        issue_step<K>(sAb, sB + kTc64Slices * S::B_BYTES, tmem + set);
-        tc::mma_commit(&tb.mma[1]);
-      }
-      __syncwarp();
-      if (tn < ntiles) load_tile(tn, b);
-    } else {
-      pendb = 1;
-      if (tn < ntiles) {
-        if (b) pendf1 = 1;
-        else pendf0 = 1;
-      }
+    if (tid == 0) {
+      issue_step<K>(sAb, sB + kTc64Slices * S::B_BYTES, tmem + set);
+      tc::mma_commit(&tb.mma[1]);
+    }
+    pendb = 1;
+    if (tn < ntiles) {
+      copy_tile(tn, b);
+      if (b) pendf1 = 1;
+      else pendf0 = 1;
     }
     has_prev = true;
     prev_base = tile_base(h, t);
     prev_set = set;
     prev_mkey = mkey;
   }
-  if (!ctl && has_prev && !tb.abort_) {
+  if (has_prev && !tb.abort_) {
     wait(&tb.mma[1], phb, pendb);
     tc::fence_after_sync();
     if (!timed_out) bra_out(prev_set, prev_base, prev_mkey);
@@ -521,7 +515,7 @@ __global__ void __launch_bounds__(kT64Threads + 32, 1)
   // ---- teardown: nothing of this block may still be in flight when its
   // tensor memory and shared memory are released (bounded, after an expiry)
   __syncthreads();
-  if (tb.abort_ && !ctl) {
+  if (tb.abort_) {
     if (pendk) tc::mbar_wait_bounded(&tb.mma[0], phk, kT64WaitPolls << 2);
     if (pendb) tc::mbar_wait_bounded(&tb.mma[1], phb, kT64WaitPolls << 2);
     if (pendf0) tc::mbar_wait_bounded(&tb.full[0], phf0, kT64WaitPolls << 2);
@@ -552,7 +546,7 @@ static cudaError_t launch_tc64_k(const LaunchArgs& a, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     configured = 1;
   }
-  k_pass_tc64<K><<<a.grid, kT64Threads + 32, t64_smem_bytes<K>(), s>>>(
+  k_pass_tc64<K><<<a.grid, kT64Threads, t64_smem_bytes<K>(), s>>>(
       static_cast<uint64_t*>(a.re), static_cast<uint64_t*>(a.im), static_cast<const TcDesc64<K>*>(a.desc), a.err);
   return cudaGetLastError();
 }
