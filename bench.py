@@ -38,6 +38,7 @@ import dmsim_workloads as W  # noqa: E402
 # writes equal to the stored runs.  Traffic grows with the state, so a launch's
 # traffic is its algorithmic bytes times this ratio.
 TRAFFIC_RATIO = 1.0003
+TRAFFIC_SOURCE = "ncu DRAM bytes of 2 launches at 12q = 1.0003 x algorithmic, scaled"
 CLASS_NAMES = {0: "MOVE", 1: "SIGNED", 2: "PHASE", 3: "DENSE", 4: "SPARSE", 5: "RLIN", 6: "SUPER", 16: "CONVERT",
                17: "TRANSPOSE", 18: "RENORM"}
 
@@ -291,6 +292,15 @@ def extra_workload(args):
         out["speedup_batched_vs_sequential"] = out["sequential_plain_s"] / out["batched_s"]
         out["diag_max_abs_err_vs_plain"] = worst
         b.close()
+    elif args.workload == "peaks":
+        # execution-unit throughputs behind the kernels' choice of arithmetic
+        rates = E.probe_rates()
+        sms = 152
+        clk = 2.07e9
+        out["ops_per_s"] = rates
+        out["per_sm_per_clock_at_2070MHz"] = {k: round(v / sms / clk, 2) for k, v in rates.items()}
+        out["fp64_fma_over_fp32_fma"] = rates["fp64_fma"] / rates["fp32_fma"]
+        out["int_lop3_over_fp32_fma"] = rates["int_lop3"] / rates["fp32_fma"]
     elif args.workload == "qft16":
         n = 16
         circ = W.qft_then_layers(n, 1000, seed=3)
@@ -362,7 +372,7 @@ def main():
     ap.add_argument("--impl", default="engine")
     ap.add_argument("--n", type=int, default=14)
     ap.add_argument("--gates", type=int, default=2000)
-    ap.add_argument("--planner", default="learned")
+    ap.add_argument("--planner", default="greedy")
     ap.add_argument("--max-k", type=int, default=4)
     ap.add_argument("--tensor", default="1", help="tensor-core passes: 0 off, 1 planner's choice, all")
     ap.add_argument("--cpu-budget", type=float, default=None,
@@ -370,8 +380,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--no-16q", action="store_true", help="skip the 16-qubit configuration")
     ap.add_argument("--workload", default="table14",
-                    help="table14 (the bench line), or extra measurements: sweep, qft16, c64_17")
+                    help="table14 (the bench line), or extra measurements: sweep, qft16, c64_17, peaks")
     args = ap.parse_args()
     if args.workload != "table14":
         return extra_workload(args)
@@ -398,10 +409,10 @@ def main():
         dist.init_process_group("nccl")
 
     hbm_peak, peak_kind = peaks()
-
-    # ---- fused path: the timed steps
     tensor = "all" if args.tensor == "all" else int(args.tensor)
-    fused = E.Simulation(n, mode="fused", max_k=args.max_k, planner=args.planner, tensor=tensor)
+
+    # ---- fused path, FP64 width (the headline): the timed steps
+    fused = E.Simulation(n, mode="fused", max_k=args.max_k, planner=args.planner, tensor=tensor, fused_arith="fp64")
     t_up0 = time.perf_counter()
     fused.extend(circ)
     fused.upload()
@@ -428,50 +439,56 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         step_ms = float(t.item())
     bytes_per_run = fused.last_timings()["bytes"]
-    launches_per_run = int(fused.last_timings()["passes"])  # pass kernels + the two double-float conversions
+    launches_per_run = int(fused.last_timings()["passes"])
 
     # ---- per-pass profile of one fused run (untimed): the dominant kernel
-    kernels, dom, _ = class_profile(fused, "df64")
+    kernels, dom, _ = class_profile(fused, "double")
     dom_name, dcount = dom["kernel"], dom["launches"]
+    if dom["tc"]:
+        dom_name = dom_name.replace("k_pass_tc<", "k_pass_tc64<")
     achieved = dom["bytes"] / (dom["ms"] * 1e-3) / 1e9
 
-    # the fixed-width greedy planner on the same circuit (the learned planner's fallback)
-    greedy_s = greedy_passes = None
-    if args.planner == "learned" and not args.no_plain:
-        g = E.Simulation(n, mode="fused", max_k=args.max_k, planner="greedy", tensor=tensor)
+    extra = {}
+    err = None
+    plain_s = plain_bytes = plain_passes = plain_kernels = None
+    if not args.no_plain:
+        # the other planner on the same circuit
+        other = "greedy" if args.planner == "learned" else "learned"
+        g = E.Simulation(n, mode="fused", max_k=args.max_k, planner=other, tensor=tensor, fused_arith="fp64")
         g.extend(circ)
         g.upload()
-        greedy_s = timed_runs(g, 1, 1) / 1e3
-        greedy_passes = g.plan_stats()[0]
+        extra[f"{other}_s"] = timed_runs(g, 1, 2) / 1e3
+        extra[f"{other}_passes"] = g.plan_stats()[0]
         g.close()
-
-    # ---- plain path (the reference's method) and the fused-vs-plain error
-    plain_s = None
-    err = None
-    plain_bytes = None
-    plain_passes = None
-    plain_fp64_s = plain_fp64_bytes = plain_fp64_err = None
-    plain_kernels = plain_fp64_kernels = None
-    if not args.no_plain:
-        plain = E.Simulation(n, mode="plain")  # double-float passes, FP64 state
+        # plain path (the reference's method, FP64 arithmetic) and the fused-vs-plain error
+        plain = E.Simulation(n, mode="plain", plain_arith="fp64")
         plain.extend(circ)
         plain.upload()
-        plain_kernels, _, plain_ms = class_profile(plain, "df64")  # per-pass events cost ~us per 1.3 ms pass
+        plain_kernels, _, plain_ms = class_profile(plain, "double")  # per-pass events cost ~us per pass
         plain_s = plain_ms / 1e3
         plain_bytes = plain.last_timings()["bytes"]
         plain_passes = plain.plan_stats()[0]
         fused.reset_dm()
         fused.run()
         err = fused.compare(plain)
-        # the same plain method with FP64 passes: bound by the FP64 pipe
-        pdf = E.Simulation(n, mode="plain", plain_arith="fp64")
+        # the double-float variants (48-bit significands, not FP64 width)
+        pdf = E.Simulation(n, mode="plain", plain_arith="df64")
         pdf.extend(circ)
         pdf.upload()
-        plain_fp64_kernels, _, pdf_ms = class_profile(pdf, "double")
-        plain_fp64_s = pdf_ms / 1e3
-        plain_fp64_bytes = pdf.last_timings()["bytes"]
-        plain_fp64_err = plain.compare(pdf)
+        extra["plain_df64_kernels"], _, pdf_ms = class_profile(pdf, "df64")
+        extra["plain_df64_s"] = pdf_ms / 1e3
+        extra["hbm_GBps_plain_df64_run"] = pdf.last_timings()["bytes"] / (pdf_ms * 1e-3) / 1e9
+        extra["plain_df64_vs_plain_error"] = plain.compare(pdf)
         pdf.close()
+        fdf = E.Simulation(n, mode="fused", max_k=args.max_k, planner="learned", tensor=tensor, fused_arith="df64")
+        fdf.extend(circ)
+        fdf.upload()
+        extra["fused_df64_s"] = timed_runs(fdf, 2, 2) / 1e3
+        extra["fused_df64_kernels"], _, _ = class_profile(fdf, "df64")
+        fdf.reset_dm()
+        fdf.run()
+        extra["fused_df64_vs_plain_error"] = fdf.compare(plain)
+        fdf.close()
         plain.close()
 
     # ---- end to end through the C ABI with host buffers
@@ -479,7 +496,6 @@ def main():
     pre = E.PinnedBuffer(N)
     pim = E.PinnedBuffer(N)
     e2e = []
-    desc_bytes = 0
     for _ in range(args.e2e_steps):
         t0 = time.perf_counter()
         fused.reset()                 # clear the circuit, rho = |0..0><0..0|
@@ -500,6 +516,13 @@ def main():
         cpu = {"value": v, "unit": "s/circuit", "cores": threads, "kind": "port", "cpu": cpu_model(),
                "sample": sample}
         parity = oracle_parity(n, circ, fused)
+    fused.close()
+
+    # ---- the 16-qubit FP64 configuration: QFT ladder on an X-Bernoulli input,
+    # then 1000 U3/CX layer gates (68.7 GB of state)
+    q16 = None
+    if rank == 0 and not args.no_16q:
+        q16 = config16(args, tensor, not args.no_plain, not args.no_cpu)
 
     if rank == 0:
         # whole-job aggregate: the world's ranks each ran one circuit per step
@@ -508,27 +531,24 @@ def main():
             "metric": METRIC,
             "value": value, "unit": "s/circuit", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "df64", "data": "synthetic (seeded circuits, state from |0..0><0..0|)",
+            "dtype": "f64", "data": "synthetic (seeded circuits, state from |0..0><0..0|)",
             "config": {"workload": f"{n}-qubit mixed-gate circuit: table_mix n={n} gates={len(circ)} seed=2 (29-entry table, random distinct qubits)",
                        "planner": args.planner, "max_k": args.max_k, "tensor": args.tensor, "passes": npasses,
                        "basic_gates": nbasic,
                        "l2": "inputs larger than L2 (rho = %.1f GB)" % (16.0 * N / 1e9), "parallelism": "replicas"},
-            "state": "FP64 rho in and out; fused and plain passes compute in double-float (FP32 hi+lo pairs), "
-                     "dense 3/4-qubit fused passes on the tensor cores; plain_fp64_* = the plain path in FP64",
+            "state": "FP64 rho in and out; fused passes at FP64 width: 3/4-qubit operators on the tensor cores "
+                     "with 7 BF16 digits per operand, exact integer order sums and one rounding to FP64 per output "
+                     "(55-bit significands per column), other passes in FP64; plain = the reference's method in FP64",
             "plain_s": plain_s, "plain_passes": plain_passes, "plain_kernels": plain_kernels,
-            "greedy_s": greedy_s, "greedy_passes": greedy_passes,
             "speedup_fused_vs_plain": (plain_s / value) if plain_s else None,
             "fused_vs_plain_error": err,
             "hbm_GBps_fused_run": bytes_per_run / (step_ms * 1e-3) / 1e9,
             "hbm_GBps_plain_run": (plain_bytes / plain_s / 1e9) if plain_s else None,
-            "plain_fp64_s": plain_fp64_s,
-            "hbm_GBps_plain_fp64_run": (plain_fp64_bytes / plain_fp64_s / 1e9) if plain_fp64_s else None,
-            "plain_vs_plain_fp64_error": plain_fp64_err, "plain_fp64_kernels": plain_fp64_kernels,
+            **extra,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": hbm_peak,
                          "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
                          "traffic": round(dom["bytes"] / dcount * TRAFFIC_RATIO),
-                         "traffic_source": "ncu DRAM bytes of 2 launches at 12q = 1.0003 x algorithmic, scaled",
-                         "peak_kind": peak_kind, "launches": dcount},
+                         "traffic_source": TRAFFIC_SOURCE, "peak_kind": peak_kind, "launches": dcount},
             "kernels": kernels,
             "e2e": {"value": float(np.mean(e2e)), "unit": "s/circuit",
                     "h2d_bytes_per_step": int(upload_bytes), "d2h_bytes_per_step": int(16 * N)},
@@ -538,11 +558,43 @@ def main():
             "wall_s_timed": wall,
             "cpu_baseline": cpu,
             "parity_vs_statevector_oracle": parity,
+            "config_16q": q16,
         }
         print(json.dumps(line))
-    fused.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+def config16(args, tensor, with_plain, with_oracle):
+    """The 16-qubit FP64 configuration beside the bench line: learned-fused
+    (FP64 width) time, the plain FP64 path's time, their difference and, in
+    the CPU leg, the fused result against the statevector oracle."""
+    import dmsim_gb300 as E
+    n = 16
+    circ = W.qft_then_layers(n, 1000, seed=3)
+    out = {"workload": "16-qubit QFT ladder on an X-Bernoulli(0.5) input + 1000 U3/CX layer gates, seed 3"}
+    f = E.Simulation(n, mode="fused", max_k=args.max_k, planner=args.planner, tensor=tensor, fused_arith="fp64")
+    f.extend(circ)
+    f.upload()
+    out["fused_s"] = timed_runs(f, 1, 2) / 1e3
+    out["fused_passes"], out["basic_gates"] = f.plan_stats()
+    out["fused_GBps"] = f.last_timings()["bytes"] / out["fused_s"] / 1e9
+    if with_plain:
+        p = E.Simulation(n, mode="plain", plain_arith="fp64")
+        p.extend(circ)
+        p.upload()
+        p.run()
+        out["plain_s"] = p.last_timings()["ms"] / 1e3
+        out["plain_GBps"] = p.last_timings()["bytes"] / out["plain_s"] / 1e9
+        out["speedup_fused_vs_plain"] = out["plain_s"] / out["fused_s"]
+        f.reset_dm()
+        f.run()
+        out["fused_vs_plain_error"] = f.compare(p)
+        p.close()
+    if with_oracle:
+        out["parity_vs_statevector_oracle"] = oracle_parity(n, circ, f)
+    f.close()
+    return out
 
 
 if __name__ == "__main__":

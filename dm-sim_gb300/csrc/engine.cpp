@@ -72,8 +72,8 @@ struct dmsim_sim {
   cudaGraphExec_t gexec = nullptr;
 
   int mode = 0, maxk = 4, planner = 0, record = 0, graph_on = 1, verbose = 0;
-  int fused_arith = 1;  // fused FP64 runs compute in double-float (1) or FP64 (0)
-  int plain_arith = 1;  // plain FP64 runs compute in double-float (1: HBM-bound) or FP64 (0: FP64-pipe-bound)
+  int fused_arith = 0;  // fused FP64 runs: FP64 width (0: FP64-width tensor passes, FP64 elsewhere) or double-float (1)
+  int plain_arith = 0;  // plain FP64 runs compute in FP64 (0: FP64-pipe-bound) or double-float (1: HBM-bound)
   int renorm = 64;      // complex64: renormalise every renorm passes (0 = never)
   int tensor = 1;       // K = 3, 4 dense/sparse passes on the tensor cores (DMSIM_OPT_TENSOR)
   int direct1 = 1;      // 1-qubit passes on the register kernel (DMSIM_OPT_DIRECT1)

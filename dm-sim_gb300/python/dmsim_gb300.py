@@ -130,13 +130,15 @@ class Simulation:
 
     ``precision`` is "fp64" or "c64"; ``mode`` is "plain" (one pass per basic
     gate, the reference's method) or "fused"; ``planner`` is "greedy" or
-    "learned" (fused mode only); ``tensor`` runs double-float 3- and 4-qubit
-    dense passes on the tensor cores (True: where the planner's rule or cost
-    model picks them, "all" or 2: every eligible pass, False: none).
+    "learned" (fused mode only); ``tensor`` runs 3- and 4-qubit dense passes
+    on the tensor cores (True: where the planner's rule or cost model picks
+    them, "all" or 2: every eligible pass, False: none); ``fused_arith`` and
+    ``plain_arith`` are "fp64" (FP64 width, the default) or "df64"
+    (double-float, 48-bit significands, faster).
     """
 
     def __init__(self, n_qubits, n_gpus=1, precision="fp64", mode="plain", max_k=4, planner="greedy",
-                 graph=True, fused_arith="df64", renorm=64, plain_arith="df64", tensor=True, direct1=True):
+                 graph=True, fused_arith="fp64", renorm=64, plain_arith="fp64", tensor=True, direct1=True):
         self._h = ctypes.c_void_p()
         self.n = int(n_qubits)
         st = lib().dmsim_create(self.n, int(n_gpus), ctypes.byref(self._h))

@@ -42,14 +42,16 @@ enum dmsim_option {
   DMSIM_OPT_SEED = 6,       /* seed of measure() without uniforms; -1 = time(0) like the reference [-1] */
   DMSIM_OPT_GRAPH = 7,      /* 1 = replay uploaded circuits from a captured CUDA graph [1] */
   DMSIM_OPT_VERBOSE = 8,    /* 1 = print the reference's per-run timing banner [0] */
-  DMSIM_OPT_FUSED_ARITH = 9, /* fused FP64 runs: 1 = double-float passes on the FP32 pipe [1], 0 = FP64 passes */
+  DMSIM_OPT_FUSED_ARITH = 9, /* fused FP64 runs: 0 = FP64 width [0] (3/4-qubit passes on the tensor cores with
+                                 7 BF16 digits per operand and exact integer sums, the rest in FP64), 1 = double-float
+                                 passes on the FP32 pipe and tensor cores (48-bit significands) */
   DMSIM_OPT_RENORM = 10,     /* complex64: FP64 trace + Hermitian renormalisation every R passes and at the end [64]; 0 = off */
-  DMSIM_OPT_PLAIN_ARITH = 11, /* plain FP64 runs (FP64 state at rest): 1 = double-float passes on the FP32 pipe [1],
-                                 0 = FP64 passes (bound by GB300's FP64 pipe) */
-  DMSIM_OPT_TENSOR = 12,      /* 3- and 4-qubit dense/sparse passes on the tensor cores (BF16 slices, exact
-                                 FP32 sums): 1 = where the learned planner (or, greedy, a density rule)
-                                 picks them in double-float runs [1], 0 = FP32 pipe only, 2 = every eligible
-                                 pass, double-float or complex64 */
+  DMSIM_OPT_PLAIN_ARITH = 11, /* plain FP64 runs (FP64 state at rest): 0 = FP64 passes [0] (dense passes bound by
+                                 GB300's FP64 pipe), 1 = double-float passes on the FP32 pipe (HBM-bound) */
+  DMSIM_OPT_TENSOR = 12,      /* 3- and 4-qubit dense/sparse passes on the tensor cores (BF16 digits, exact
+                                 FP32 sums): 1 = where the learned planner picks them, else every eligible
+                                 pass of an FP64-width run and, in double-float runs, passes above a density
+                                 rule [1]; 0 = never; 2 = every eligible pass, complex64 runs included */
   DMSIM_OPT_DIRECT1 = 13      /* 1 = 1-qubit move/sign/phase/dense passes on the register kernel (no shared-memory
                                  tiles) [1], 0 = the tiled kernel */
 };
