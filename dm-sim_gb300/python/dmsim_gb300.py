@@ -467,6 +467,13 @@ def cost_load(path):
     _ok(lib().dmsim_cost_load(path.encode()), "cost_load")
 
 
+def cost_load_default():
+    """Reload the model the library ships with ($DMSIM_COST_MODEL, else
+    dm-sim_gb300/model/cost_mlp.bin), e.g. after training another one."""
+    path = os.environ.get("DMSIM_COST_MODEL") or os.path.normpath(os.path.join(_HERE, "..", "model", "cost_mlp.bin"))
+    cost_load(path)
+
+
 def mlp_forward(params, X):
     params = np.ascontiguousarray(params, dtype=np.float32)
     X = np.ascontiguousarray(X, dtype=np.float32)

@@ -138,3 +138,19 @@ def hea_sweep(ncirc=512, seed=4, nmin=6, nmax=12, lmin=4, lmax=10):
 
 def u3_cx_ccx(n=17, ngates=1000, seed=5):
     return random_circuit(n, ngates, [OP["U3"], OP["CX"], OP["CCX"]], seed=seed)
+
+
+def sparse_triples(n=14, ngates=600, seed=6):
+    """Controlled rotations, phases and CX inside fixed disjoint qubit triples
+    (0-2, 3-5, ...), in random order across the triples: every fused block is
+    a sparse 3-qubit operator (at most 2 nonzeros per row), the case where the
+    tensor-core passes lose to the pipe kernels."""
+    rng = np.random.default_rng(seed)
+    ops = [OP["CRY"], OP["CRZ"], OP["CU1"], OP["CRX"], OP["CX"], OP["CZ"]]
+    ntri = n // 3
+    out = []
+    for _ in range(ngates):
+        t = int(rng.integers(0, ntri))
+        a, b = (int(x) for x in rng.choice(3, size=2, replace=False))
+        out.append(make_gate(int(rng.choice(ops)), (3 * t + a, 3 * t + b), rng))
+    return out

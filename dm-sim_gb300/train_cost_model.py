@@ -38,6 +38,8 @@ def main():
         # 16 qubits (68.7 GB of FP64 state): shorter circuits, the passes are ~16x slower
         circuits, gates = (args.circuits, args.gates) if n <= 14 else (2, max(8, args.gates // 2))
         for arith in (E.AR_DF64, E.AR_FP64, E.AR_FP32):
+            if arith == E.AR_FP64 and n > 14:
+                continue  # FP64-pipe dense 4-qubit passes take ~1 s each at 16 qubits; the per-entry model extrapolates
             f, m = E.cost_collect(n, n_circuits=circuits, gates=gates, seed=100 * args.seed + 10 * i + arith,
                                   arith=arith)
             feats.append(f)

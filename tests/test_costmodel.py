@@ -92,33 +92,62 @@ def test_collect_train_predict(engine, tmp_path):
 
 
 @pytest.mark.gpu
-def test_learned_planner_beats_fixed_width_greedy(engine, oracle):
-    """Train on the engine's own timings, then plan a 12-qubit mixed-table
-    circuit with the learned planner and with the greedy k<=4 planner: the
-    learned plan is no slower (measured), and both match the oracle."""
+def test_learned_planner_vs_fixed_width_greedy(engine, oracle):
+    """Train on the engine's own FP64 timings (pipe kernels and FP64-width
+    tensor passes), then plan a 12-qubit mixed-table circuit with the learned
+    planner and with the greedy k<=4 planner: both match the oracle and the
+    learned plan is no slower than the fixed rule (measured).  On GB300 the
+    fixed rule -- widest fusion, tensor cores for every dense 3/4-qubit block
+    -- is within a few percent of every plan the learned planner scores."""
     n = 12
     feats, ms = [], []
     for seed, nn in ((11, 10), (12, 12)):
-        f, m = engine.cost_collect(nn, n_circuits=2, gates=60, seed=seed)
+        f, m = engine.cost_collect(nn, n_circuits=2, gates=60, seed=seed, arith=engine.AR_FP64)
         feats.append(f)
         ms.append(m)
     engine.cost_train(np.concatenate(feats), np.concatenate(ms), steps=3000, lr=3e-3, seed=2)
-    circ = W.table_mix(n, 300, seed=77)
+    try:
+        circ = W.table_mix(n, 300, seed=77)
+        times = {}
+        states = {}
+        for planner in ("greedy", "learned"):
+            with engine.Simulation(n, mode="fused", planner=planner) as s:
+                s.extend(circ)
+                s.upload()
+                s.run()
+                t = []
+                for _ in range(3):
+                    s.reset_dm()
+                    s.run()
+                    t.append(s.last_timings()["ms"])
+                times[planner] = min(t)
+                states[planner] = s.get_dm()
+        ref = oracle.dm_sim(n, circ)
+        for st in states.values():
+            assert max(np.abs(st[0] - ref[0]).max(), np.abs(st[1] - ref[1]).max()) <= 1e-12
+        assert times["learned"] <= times["greedy"] * 1.05, times
+    finally:
+        engine.cost_load_default()
+
+
+@pytest.mark.gpu
+@pytest.mark.slow
+def test_shipped_model_gain_double_float_14q(engine):
+    """The shipped model on the 14-qubit mixed-table workload in double-float
+    arithmetic, where the fixed density rule sends some sparse 4-qubit blocks
+    to the wrong unit: the learned plan is measured faster than the greedy one
+    (3.5% when the model was trained: 3.47 s against 3.59 s)."""
+    n = 14
+    circ = W.table_mix(n, 2000, seed=2)
     times = {}
-    states = {}
     for planner in ("greedy", "learned"):
-        with engine.Simulation(n, mode="fused", planner=planner) as s:
+        with engine.Simulation(n, mode="fused", planner=planner, fused_arith="df64") as s:
             s.extend(circ)
             s.upload()
             s.run()
             t = []
-            for _ in range(3):
-                s.reset_dm()
+            for _ in range(2):
                 s.run()
                 t.append(s.last_timings()["ms"])
             times[planner] = min(t)
-            states[planner] = s.get_dm()
-    ref = oracle.dm_sim(n, circ)
-    for st in states.values():
-        assert max(np.abs(st[0] - ref[0]).max(), np.abs(st[1] - ref[1]).max()) <= 1e-10
-    assert times["learned"] <= times["greedy"] * 1.05, times
+    assert times["learned"] <= times["greedy"] * 0.99, times
