@@ -155,6 +155,39 @@ __global__ void __launch_bounds__(256) k_batch_epilogue(const T* __restrict__ re
   }
 }
 
+// One circuit held outside the batch arrays (a wide circuit, run by the
+// engine's own pass kernels): its diagonal and <Z_i Z_{i+1}>, one block.
+__global__ void __launch_bounds__(256) k_circuit_epilogue(const double* __restrict__ re, int n, double* __restrict__ diag,
+                                                          double* __restrict__ zz) {
+  const uint64_t dim = 1ull << n;
+  double acc[kBatchMaxQubits];
+#pragma unroll
+  for (int i = 0; i < kBatchMaxQubits; i++) acc[i] = 0;
+  for (uint64_t r = threadIdx.x; r < dim; r += blockDim.x) {
+    const double d = re[r * dim + r];
+    diag[r] = d;
+#pragma unroll
+    for (int i = 0; i < kBatchMaxQubits - 1; i++)
+      if (i < n - 1) acc[i] += (((r >> i) ^ (r >> (i + 1))) & 1) ? -d : d;
+  }
+  __shared__ double s[256];
+  for (int i = 0; i < n - 1; i++) {
+    s[threadIdx.x] = acc[i];
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+      if (threadIdx.x < st) s[threadIdx.x] += s[threadIdx.x + st];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) zz[i] = s[0];
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_circuit_epilogue(const double* re, int n, double* diag, double* zz, cudaStream_t s) {
+  k_circuit_epilogue<<<1, 256, 0, s>>>(re, n, diag, zz);
+  return cudaGetLastError();
+}
+
 template <typename T, int K>
 static size_t smem_k() {
   size_t m = 0;
@@ -194,6 +227,7 @@ static cudaError_t launch_t(const BatchLaunch& a, cudaStream_t s) {
                              (int)cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
   // all-zero bytes are 0 in both FP64 and double-float
+  if (a.ncirc == 0) return cudaSuccess;  // every circuit is a wide one
   e = cudaMemsetAsync(a.re, 0, a.total_entries * sizeof(double), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(a.im, 0, a.total_entries * sizeof(double), s);
   if (e != cudaSuccess) return e;

@@ -45,6 +45,9 @@ struct BatchLaunch {
 size_t batch_smem_bytes();
 int batch_blocks_per_sm(bool df64_arith);
 // memset states, rho_c = |0><0|, reset the queue, the work-queue kernel, the epilogue
+// (circs: the circuits held in the batch arrays; nothing when ncirc is 0)
 cudaError_t launch_batch(const BatchLaunch& a, cudaStream_t s);
+// diag[0..2^n) and zz[0..n-1) of one FP64 state held elsewhere (one block)
+cudaError_t launch_circuit_epilogue(const double* re, int n, double* diag, double* zz, cudaStream_t s);
 
 }  // namespace dmg

@@ -137,27 +137,27 @@ void check_qubits(const dmsim_sim* s, const GateRec& g) {
       if (g.qb[i] == g.qb[j]) throw DmError{DMSIM_ERR_ARG, "a gate's qubits must be distinct"};
 }
 
-// Launch the planned passes on the stream (captured or direct).
-void enqueue_passes(dmsim_sim* s, bool timed) {
+// Launch the planned passes on stream st (captured or direct).
+void enqueue_passes(dmsim_sim* s, bool timed, cudaStream_t st) {
   for (size_t i = 0; i < s->passes.size(); i++) {
     PassInfo& p = s->passes[i];
     if (p.renorm) {
-      if (timed) DM_CUDA(cudaEventRecord(p.ev0, s->stream));
-      DM_CUDA(launch_renormalise(s->d_re, s->d_im, (int)s->n, s->fp32, s->d_acc + 4, p.grid, s->stream));
-      if (timed) DM_CUDA(cudaEventRecord(p.ev1, s->stream));
+      if (timed) DM_CUDA(cudaEventRecord(p.ev0, st));
+      DM_CUDA(launch_renormalise(s->d_re, s->d_im, (int)s->n, s->fp32, s->d_acc + 4, p.grid, st));
+      if (timed) DM_CUDA(cudaEventRecord(p.ev1, st));
       continue;
     }
     if (p.conv) {
-      if (timed) DM_CUDA(cudaEventRecord(p.ev0, s->stream));
-      if (p.conv == 1) DM_CUDA(launch_to_df64(s->d_re, s->d_im, s->N, p.grid, s->stream));
-      else DM_CUDA(launch_from_df64(s->d_re, s->d_im, s->N, p.grid, s->stream));
-      if (timed) DM_CUDA(cudaEventRecord(p.ev1, s->stream));
+      if (timed) DM_CUDA(cudaEventRecord(p.ev0, st));
+      if (p.conv == 1) DM_CUDA(launch_to_df64(s->d_re, s->d_im, s->N, p.grid, st));
+      else DM_CUDA(launch_from_df64(s->d_re, s->d_im, s->N, p.grid, st));
+      if (timed) DM_CUDA(cudaEventRecord(p.ev1, st));
       continue;
     }
     if (p.transpose) {
-      if (timed) DM_CUDA(cudaEventRecord(p.ev0, s->stream));
-      DM_CUDA(launch_conj_transpose(s->d_re, s->d_im, (int)s->n, s->fp32, p.grid, s->stream));
-      if (timed) DM_CUDA(cudaEventRecord(p.ev1, s->stream));
+      if (timed) DM_CUDA(cudaEventRecord(p.ev0, st));
+      DM_CUDA(launch_conj_transpose(s->d_re, s->d_im, (int)s->n, s->fp32, p.grid, st));
+      if (timed) DM_CUDA(cudaEventRecord(p.ev1, st));
       continue;
     }
     LaunchArgs a;
@@ -176,9 +176,9 @@ void enqueue_passes(dmsim_sim* s, bool timed) {
     a.direct1 = p.direct1;
     a.q0 = p.q0;
     a.n = (int)s->n;
-    if (timed) DM_CUDA(cudaEventRecord(p.ev0, s->stream));
-    DM_CUDA(launch_pass(a, s->stream));
-    if (timed) DM_CUDA(cudaEventRecord(p.ev1, s->stream));
+    if (timed) DM_CUDA(cudaEventRecord(p.ev0, st));
+    DM_CUDA(launch_pass(a, st));
+    if (timed) DM_CUDA(cudaEventRecord(p.ev1, st));
   }
 }
 
@@ -346,7 +346,7 @@ void upload_specs(dmsim_sim* s, const std::vector<PassSpec>& specs, uint32_t n_b
     cudaGraph_t graph = nullptr;
     DM_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
     try {
-      enqueue_passes(s, false);
+      enqueue_passes(s, false, s->stream);
     } catch (...) {
       cudaStreamEndCapture(s->stream, &graph);
       if (graph) cudaGraphDestroy(graph);
@@ -374,7 +374,7 @@ void run(dmsim_sim* s) {
     }
   }
   DM_CUDA(cudaEventRecord(s->ev0, s->stream));
-  if (timed || !s->gexec) enqueue_passes(s, timed);
+  if (timed || !s->gexec) enqueue_passes(s, timed, s->stream);
   else DM_CUDA(cudaGraphLaunch(s->gexec, s->stream));
   DM_CUDA(cudaEventRecord(s->ev1, s->stream));
   DM_CUDA(cudaEventSynchronize(s->ev1));
@@ -1274,3 +1274,36 @@ const char* dmsim_status_string(int st) {
 }
 
 }  // extern "C"
+
+namespace dmg {
+
+cudaError_t sim_enqueue(dmsim_handle s, cudaStream_t st, std::string& err) {
+  if (!s || !s->uploaded) {
+    err = "sim_enqueue: no uploaded plan";
+    return cudaErrorInvalidValue;
+  }
+  try {
+    DM_CUDA(launch_set_zero_state(s->d_re, s->d_im, s->N, s->fp32, st));
+    enqueue_passes(s, false, st);
+  } catch (const DmError& e) {
+    err = e.msg;
+    return cudaErrorUnknown;
+  }
+  return cudaSuccess;
+}
+
+double sim_plan_bytes(dmsim_handle s) {
+  double t = 0;
+  for (const PassInfo& p : s->passes) t += p.bytes;
+  return t;
+}
+
+cudaError_t sim_take_error(dmsim_handle s, int* flag) {
+  int h = 0;
+  cudaError_t e = cudaMemcpy(&h, s->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && h) e = cudaMemset(s->d_err, 0, sizeof(int));
+  *flag = h;
+  return e;
+}
+
+}  // namespace dmg

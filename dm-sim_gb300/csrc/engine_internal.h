@@ -3,6 +3,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
+#include "../../include/dmsim_gb300.h"
 #include "plan.h"
 
 namespace dmg {
@@ -34,5 +37,13 @@ struct PassRecord {
   double bytes;
   unsigned grid;
 };
+
+// For the batched sweep (batch.cpp): enqueue |0..0><0..0| and every pass of
+// s's uploaded plan on stream st (e.g. inside another stream's capture), and
+// read-and-clear s's device error flag (set by an expired bounded wait).
+cudaError_t sim_enqueue(dmsim_handle s, cudaStream_t st, std::string& err);
+cudaError_t sim_take_error(dmsim_handle s, int* flag);
+// algorithmic bytes of s's uploaded plan (reads + writes of every pass)
+double sim_plan_bytes(dmsim_handle s);
 
 }  // namespace dmg

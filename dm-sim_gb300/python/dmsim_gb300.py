@@ -16,7 +16,7 @@ OK, ERR_ARG, ERR_STATE, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_UNSUPPORTED = range(
 (OPT_MODE, OPT_PRECISION, OPT_MAX_K, OPT_PLANNER, OPT_RECORD, OPT_SEED, OPT_GRAPH, OPT_VERBOSE, OPT_FUSED_ARITH,
  OPT_RENORM, OPT_PLAIN_ARITH, OPT_TENSOR, OPT_DIRECT1) = range(1, 14)
 AR_FP64, AR_FP32, AR_DF64 = 0, 1, 2
-BATCH_OPT_WAIT_LIMIT, BATCH_OPT_TEST_STALL = 100, 101
+BATCH_OPT_WAIT_LIMIT, BATCH_OPT_TEST_STALL, BATCH_OPT_WIDE_QUBITS = 100, 101, 102
 PASS_RECORD = 10  # doubles per pass record: K, class, nnz, max_lo_bit, min_hi_bit, n, ms, bytes, tensor, blocks
 
 OP_NAMES = ["U3", "U2", "U1", "CX", "ID", "X", "Y", "Z", "H", "S",
@@ -509,11 +509,13 @@ def probe_rates():
 
 class Batch:
     """Many independent circuits (1..16 qubits each, uneven counts allowed),
-    each from |0..0><0..0|, run together by one persistent work-queue kernel
-    from one captured CUDA graph.  Outputs per circuit: the diagonal and
-    <Z_i Z_{i+1}>."""
+    each from |0..0><0..0|, run together from one captured CUDA graph: the
+    circuits below ``wide_qubits`` (default 10) by one persistent work-queue
+    kernel, each wider one by the engine's own pass kernels on a concurrent
+    branch.  Outputs per circuit: the diagonal and <Z_i Z_{i+1}>."""
 
-    def __init__(self, n_qubits_list, mode="fused", max_k=4, planner="greedy", wait_limit=None, test_stall=False):
+    def __init__(self, n_qubits_list, mode="fused", max_k=4, planner="greedy", wait_limit=None, test_stall=False,
+                 fused_arith="fp64", wide_qubits=None):
         self.nq = [int(x) for x in n_qubits_list]
         self._h = ctypes.c_void_p()
         arr = (ctypes.c_uint32 * len(self.nq))(*self.nq)
@@ -527,6 +529,9 @@ class Batch:
             self._check(lib().dmsim_batch_set_option(self._h, BATCH_OPT_WAIT_LIMIT, int(wait_limit)))
         if test_stall:
             self._check(lib().dmsim_batch_set_option(self._h, BATCH_OPT_TEST_STALL, 1))
+        self._check(lib().dmsim_batch_set_option(self._h, OPT_FUSED_ARITH, 1 if fused_arith == "df64" else 0))
+        if wide_qubits is not None:
+            self._check(lib().dmsim_batch_set_option(self._h, BATCH_OPT_WIDE_QUBITS, int(wide_qubits)))
 
     def _check(self, st):
         if st != OK:

@@ -202,14 +202,17 @@ int dmsim_mlp_forward(const float* params, const float* X, uint32_t B, float* y)
 int dmsim_mlp_grad(const float* params, const float* X, const float* T, uint32_t B, float* grad, float* loss);
 /* Predicted run time of the uploaded plan (learned planner), ms */
 int dmsim_plan_predicted_ms(dmsim_handle h, double* ms);
-/* ---- batched sweep: many independent circuits in one persistent launch ----
+/* ---- batched sweep: many independent circuits in one captured graph -------
  * Circuits of 1..16 qubits (uneven counts allowed), each from |0..0><0..0|,
- * planned like single circuits (DMSIM_OPT_MODE / MAX_K / PLANNER via
- * dmsim_batch_set_option), run by one work-queue kernel replayed from a
- * captured CUDA graph.  Outputs per circuit: the diagonal (2^n) and
- * <Z_i Z_{i+1}> for i < n-1.  stats: {ms of the last run, passes, basic
- * gates, work items, algorithmic bytes, grid, tile-shape small_n, g_shift}.  No reference counterpart: the
- * reference runs circuits one Simulation at a time. */
+ * planned like single circuits (DMSIM_OPT_MODE / MAX_K / PLANNER /
+ * FUSED_ARITH via dmsim_batch_set_option), run from one captured CUDA graph:
+ * the narrow circuits (fewer than DMSIM_BATCH_OPT_WIDE_QUBITS qubits) by one
+ * persistent work-queue kernel, each wide circuit by the engine's own pass
+ * kernels on a concurrent branch.  Outputs per circuit: the diagonal (2^n)
+ * and <Z_i Z_{i+1}> for i < n-1.  stats: {ms of the last run, passes, basic
+ * gates, work items of the queue, algorithmic bytes, queue grid, tile-shape
+ * small_n, g_shift}.  No reference counterpart: the reference runs circuits
+ * one Simulation at a time. */
 typedef struct dmsim_batch* dmsim_batch_handle;
 /* Batch-only options: the polls (128 ns naps) after which a work-queue
  * dependency wait gives up [2^25, ~4 s] -- the kernel then sets an error flag,
@@ -218,7 +221,10 @@ typedef struct dmsim_batch* dmsim_batch_handle;
  * set to NaN -- and a test hook that makes the last pass of circuit 0
  * wait for one tile more than its predecessor has, so that its waits run
  * out (failure detection without a GPU fault). */
-enum { DMSIM_BATCH_OPT_WAIT_LIMIT = 100, DMSIM_BATCH_OPT_TEST_STALL = 101 };
+enum { DMSIM_BATCH_OPT_WAIT_LIMIT = 100, DMSIM_BATCH_OPT_TEST_STALL = 101,
+       /* circuits of at least this many qubits run on the engine's own pass kernels (tensor-core passes
+          included), as concurrent branches of the batch's graph; the rest share the work-queue kernel [10] */
+       DMSIM_BATCH_OPT_WIDE_QUBITS = 102 };
 int dmsim_batch_create(uint32_t n_circuits, const uint32_t* n_qubits, dmsim_batch_handle* out);
 int dmsim_batch_destroy(dmsim_batch_handle b);
 int dmsim_batch_set_option(dmsim_batch_handle b, int key, int64_t value);
@@ -229,8 +235,9 @@ int dmsim_batch_run(dmsim_batch_handle b);
 int dmsim_batch_get_diag(dmsim_batch_handle b, uint32_t circuit, double* out);
 int dmsim_batch_get_zz(dmsim_batch_handle b, uint32_t circuit, double* out);
 int dmsim_batch_get_dm(dmsim_batch_handle b, uint32_t circuit, double* re, double* im);
-/* The tile-shape autotuner: times the uploaded batch under a few tile shapes
- * (fewer groups per tile for the small circuits) and keeps the fastest. */
+/* The autotuner: times the uploaded batch under a few choices of the wide
+ * circuits' threshold and of the queue's tile shape (fewer groups per tile
+ * for its smallest circuits) and keeps the fastest. */
 int dmsim_batch_autotune(dmsim_batch_handle b, double* best_ms);
 int dmsim_batch_stats(dmsim_batch_handle b, double out[8]);
 const char* dmsim_batch_last_error(dmsim_batch_handle b);

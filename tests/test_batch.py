@@ -43,6 +43,29 @@ def test_batch_matches_oracle(engine, oracle, mode):
                     assert np.abs(b.zz(c) - zz_from_diag(rd, n)).max() <= 10 * tol
 
 
+@pytest.mark.parametrize("arith", ["fp64", "df64"])
+def test_wide_circuits_on_engine_kernels(engine, oracle, arith):
+    """Circuits at or above the wide threshold run on the engine's own pass
+    kernels (tensor-core passes included) as concurrent graph branches, the
+    rest in the work-queue kernel; both kinds against the oracle, twice."""
+    rng = np.random.default_rng(8)
+    sweep = [(n, W.hea(n, 3, rng)) for n in (4, 7, 5, 8, 6, 9, 7)]
+    with engine.Batch([n for n, _ in sweep], mode="fused", fused_arith=arith, wide_qubits=7) as b:
+        for c, (n, circ) in enumerate(sweep):
+            b.extend(c, circ)
+        b.upload()
+        for _ in range(2):
+            b.run()
+            for c, (n, circ) in enumerate(sweep):
+                ref = oracle.dm_sim(n, circ)
+                re, im = b.dm(c)
+                assert max(np.abs(re - ref[0]).max(), np.abs(im - ref[1]).max()) <= 1e-10, (c, n)
+                d = 1 << n
+                rd = ref[0].reshape(d, d).diagonal()
+                assert np.abs(b.diag(c) - rd).max() <= 1e-10
+                assert np.abs(b.zz(c) - zz_from_diag(rd, n)).max() <= 1e-9
+
+
 def test_hea_sweep_shape(engine, oracle):
     """The parameter-sweep workload's shape (HEA, qubits uniform in {6..12}),
     64 circuits: every output against the oracle's diagonal."""
