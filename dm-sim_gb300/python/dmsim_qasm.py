@@ -99,9 +99,15 @@ def _split_args(s):
 _STMT = re.compile(r"^([A-Za-z_][A-Za-z0-9_]*)\s*(?:\((.*)\))?\s*(.*)$", re.S)
 
 
-def parse_qasm(text):
+def parse_qasm(text, conditionals="error"):
     """Returns (n_qubits, circuit, measured) where circuit holds
-    (op, qubits, theta, phi, lam) tuples for the engine."""
+    (op, qubits, theta, phi, lam) tuples for the engine.  A density matrix has
+    no single measured outcome to branch on, so classically controlled
+    statements (``if(c==k) ...;``) and ``reset`` raise QasmError, unless
+    ``conditionals="skip"``: then they are dropped, gate included, as the
+    reference's translator does (tool/dmsim_qasm.py:104, :321-322)."""
+    if conditionals not in ("error", "skip"):
+        raise ValueError("conditionals must be 'error' or 'skip'")
     text = re.sub(r"//[^\n]*", "", text)
     # gate definitions first (their bodies hold ';')
     gates = {}
@@ -191,6 +197,8 @@ def parse_qasm(text):
             src = stmt[len("measure"):].split("->")[0]
             measured.extend(qubits_of(src))
             continue
+        if conditionals == "skip" and (stmt.startswith("reset") or re.match(r"if\s*\(", stmt)):
+            continue
         if stmt.startswith(("reset", "if", "opaque")):
             raise QasmError(f"unsupported statement: {stmt.split()[0]}")
         m = _STMT.match(stmt)
@@ -205,7 +213,7 @@ def parse_qasm(text):
     return nq, circuit, measured
 
 
-def load_qasm(path_or_text, **sim_options):
+def load_qasm(path_or_text, conditionals="error", **sim_options):
     """Parse a QASM file (or program text) into a new engine Simulation,
     uploaded and ready to run.  Returns (simulation, measured qubits)."""
     import dmsim_gb300 as E
@@ -213,7 +221,7 @@ def load_qasm(path_or_text, **sim_options):
     if "\n" not in path_or_text and path_or_text.endswith(".qasm"):
         with open(path_or_text) as f:
             text = f.read()
-    n, circ, measured = parse_qasm(text)
+    n, circ, measured = parse_qasm(text, conditionals=conditionals)
     sim = E.Simulation(n, **sim_options)
     sim.extend(circ)
     sim.upload()
