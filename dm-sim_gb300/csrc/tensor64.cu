@@ -80,6 +80,10 @@ struct T64Tables {
   uint32_t stmask[8];
   int lk[D], lb[D];
   int ew[2][D];
+  // output (a, b) of a tile: bits 0..47 its offset from the tile base minus
+  // the free bits, bits 48..55 the bra row exponent ew[1][b] + 128, bit 63
+  // set when its run is stored
+  uint64_t outoff[D][D];
   uint32_t colmax[4][128];  // per quarter and column: largest FP64 exponent field
   uint32_t brmax[2][128];   // per tile parity and bra column: magnitude key of the ket outputs
   int colEt[128 / D][D];    // biased exponent of ket column (b, f)'s grid, at [f][b]
@@ -175,16 +179,23 @@ __device__ __forceinline__ uint64_t to_fp64(int64_t Y, int P) {
   return (Y != 0 && E > 0) ? b + ((uint64_t)(int64_t)P << 52) : 0ull;
 }
 
-// Pack the digits of 4 consecutive K indices of row m into the K-major
-// operand, 8 bytes per slice.
-__device__ __forceinline__ void store_digits4(unsigned char* sA, uint32_t a_bytes, uint32_t off,
-                                              const float (&dg)[4][kTc64Slices]) {
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);  // exact: |digit| <= 128
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// Store the packed digits of Q consecutive K indices of row m (pk[i][j]:
+// values 2i, 2i+1 of slice j) into the K-major operand, one 16-byte (Q = 8)
+// or 8-byte (Q = 4) store per slice.
+template <int Q>
+__device__ __forceinline__ void store_packed(unsigned char* sA, uint32_t a_bytes, uint32_t off,
+                                             const uint32_t (&pk)[Q / 2][kTc64Slices]) {
 #pragma unroll
   for (int j = 0; j < kTc64Slices; j++) {
-    const __nv_bfloat162 v0 = __floats2bfloat162_rn(dg[0][j], dg[1][j]);  // exact: |digit| <= 128
-    const __nv_bfloat162 v1 = __floats2bfloat162_rn(dg[2][j], dg[3][j]);
-    *reinterpret_cast<uint2*>(sA + j * a_bytes + off) =
-        make_uint2(*reinterpret_cast<const uint32_t*>(&v0), *reinterpret_cast<const uint32_t*>(&v1));
+    if constexpr (Q == 8)
+      *reinterpret_cast<uint4*>(sA + j * a_bytes + off) = make_uint4(pk[0][j], pk[1][j], pk[2][j], pk[3][j]);
+    else
+      *reinterpret_cast<uint2*>(sA + j * a_bytes + off) = make_uint2(pk[0][j], pk[1][j]);
   }
 }
 
@@ -260,6 +271,17 @@ __global__ void __launch_bounds__(kT64Threads, 1)
     tb.ew[0][tid] = dp->ew[0][tid];
     tb.ew[1][tid] = dp->ew[1][tid];
   }
+  if (tid < D * D) {
+    const int a = tid / D, bb = tid % D;
+    int e = 0;
+    for (int i = 0; i < K; i++) e |= (((a >> i) & 1) << h.lket[i]) | (((bb >> i) & 1) << h.lbra[i]);
+    const int run = e >> h.L;
+    uint64_t off = 0;
+    for (int j = 0; j < h.mhi; j++) off |= (uint64_t)((run >> j) & 1) << h.hipos[j];
+    off += (uint64_t)(e & ((1 << h.L) - 1));
+    const uint64_t stored = (h.stmask[run >> 5] >> (run & 31)) & 1;
+    tb.outoff[a][bb] = off | ((uint64_t)(dp->ew[1][bb] + 128) << 48) | (stored << 63);
+  }
   if (tid < 128) tb.brmax[0][tid] = tb.brmax[1][tid] = 0;
   if (tid == 0) tb.abort_ = 0;
   if (w == 0) {
@@ -331,9 +353,8 @@ __global__ void __launch_bounds__(kT64Threads, 1)
 
   // the previous tile's bra outputs -> FP64 -> its stored runs
   auto bra_out = [&](uint32_t set, uint64_t base, uint32_t mkey) {
-    const int pa = (int)mkey + tb.ew[0][r] - 1106;
-    const int baseb = tb.lk[r] + lf_g;
-    uint64_t* arr = half ? im : re;
+    const int pa = (int)mkey + tb.ew[0][r] - 1106 - 128;
+    uint64_t* arr = (half ? im : re) + base + lf_g;
 #pragma unroll
     for (int c4 = 0; c4 < Q; c4 += QH) {
       float sv[kTc64Orders][QH];
@@ -343,12 +364,11 @@ __global__ void __launch_bounds__(kT64Threads, 1)
       tc::tmem_wait_ld();
 #pragma unroll
       for (int c = 0; c < QH; c++) {
+        const uint64_t T = tb.outoff[r][cb + c4 + c];
+        if (!(T >> 63)) continue;  // a run the pass does not change
         const int64_t Y =
             combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c], sv[6][c], sv[7][c]);
-        const uint64_t bits = to_fp64(Y, pa + tb.ew[1][cb + c4 + c]);
-        const int e = baseb + tb.lb[cb + c4 + c];
-        const int run = e >> L;
-        if ((tb.stmask[run >> 5] >> (run & 31)) & 1) arr[base + tb.hioff[run] + (uint64_t)(e & (runlen - 1))] = bits;
+        arr[T & 0xFFFFFFFFFFFFull] = to_fp64(Y, pa + (int)((T >> 48) & 0xFF));
       }
     }
     tc::fence_before_sync();
@@ -404,13 +424,16 @@ __global__ void __launch_bounds__(kT64Threads, 1)
       ecm = max(ecm, 64u << 20);
       Ec = (int)(ecm >> 20);
       if (q == 0) tb.colEt[f][r] = Ec;
+      uint32_t pk[Q / 2][kTc64Slices];
 #pragma unroll
-      for (int c4 = 0; c4 < Q; c4 += QH) {
-        float dg[QH][kTc64Slices];
+      for (int c2 = 0; c2 < Q / 2; c2++) {
+        float d0[kTc64Slices], d1[kTc64Slices];
+        digits_fp64(xl[2 * c2], xh[2 * c2], ecm, d0);
+        digits_fp64(xl[2 * c2 + 1], xh[2 * c2 + 1], ecm, d1);
 #pragma unroll
-        for (int c = 0; c < QH; c++) digits_fp64(xl[c4 + c], xh[c4 + c], ecm, dg[c]);
-        store_digits4(sAk, S::A_BYTES, tc_kmajor_offset(m, c0 + c4, S::SBO), dg);
+        for (int j = 0; j < kTc64Slices; j++) pk[c2][j] = pack_bf16x2(d0[j], d1[j]);
       }
+      store_packed<Q>(sAk, S::A_BYTES, tc_kmajor_offset(m, c0, S::SBO), pk);
       tc::fence_proxy_async_smem();
     }
     tc::fence_before_sync();
@@ -466,18 +489,22 @@ __global__ void __launch_bounds__(kT64Threads, 1)
       int ecol[Q];
 #pragma unroll
       for (int c = 0; c < Q; c++) ecol[c] = tb.colEt[f][cb + c];
+      uint32_t pk[Q / 2][kTc64Slices];
 #pragma unroll
-      for (int c4 = 0; c4 < Q; c4 += QH) {
-        float dg[QH][kTc64Slices];
+      for (int c2 = 0; c2 < Q / 2; c2++) {
+        float d[2][kTc64Slices];
 #pragma unroll
-        for (int c = 0; c < QH; c++) {
-          const int64_t Y = (int64_t)buf[yidx(r, cb + c4 + c)];
-          const int sh = (int)mkey - 141 - ecol[c4 + c];
+        for (int u = 0; u < 2; u++) {
+          const int c = 2 * c2 + u;
+          const int64_t Y = (int64_t)buf[yidx(r, cb + c)];
+          const int sh = (int)mkey - 141 - ecol[c];
           const int64_t v = sh >= 0 ? shr_s64(Y, (uint32_t)sh) : shl_s64(Y, (uint32_t)(-sh));
-          digits_int(v, dg[c]);
+          digits_int(v, d[u]);
         }
-        store_digits4(sAb, S::A_BYTES, tc_kmajor_offset(m, c0 + c4, S::SBO), dg);
+#pragma unroll
+        for (int j = 0; j < kTc64Slices; j++) pk[c2][j] = pack_bf16x2(d[0][j], d[1][j]);
       }
+      store_packed<Q>(sAb, S::A_BYTES, tc_kmajor_offset(m, c0, S::SBO), pk);
       // the next tile's values (its loads were issued two tiles ago)
       if (t + step < ntiles) {
         wait_full(b ^ 1);
