@@ -134,7 +134,9 @@ double* g_noalloc_addr[256] = {};  // device address of the scratch, per device 
 }  // namespace
 
 // Once per device, with that device current: look up the scratch's device
-// address.  Later calls on the device reuse it.
+// address.  Later calls on the device reuse it (for the life of the process:
+// a device reset in between would leave the cached address stale, which the
+// header tells callers not to do).
 static cudaError_t noalloc_scratch(double** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);

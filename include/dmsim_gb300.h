@@ -153,7 +153,10 @@ int dmsim_pure_metrics(dmsim_handle h, const double* psi_re, const double* psi_i
  * Every call reuses the same array (the accumulators are cleared each call,
  * psi is overwritten), so calls that overlap on the GPU -- from two threads or
  * two handles on the same device -- race; serialise them.  Same outputs as
- * dmsim_pure_metrics; rho must already be allocated (DMSIM_ERR_STATE if not). */
+ * dmsim_pure_metrics; rho must already be allocated (DMSIM_ERR_STATE if not).
+ * The array's address is looked up once per device and kept for the life of
+ * the process: do not call this entry point after cudaDeviceReset (or any
+ * other teardown of the device's primary context) in the same process. */
 int dmsim_pure_metrics_noalloc(dmsim_handle h, const double* psi_re, const double* psi_im, double out[4]);
 /* Compare two states of the same size on the device (either precision, e.g.
  * a complex64 state against an FP64 one): out[0] = max |A - B| over entries,

@@ -5,8 +5,10 @@ reserved by another allocator, or a monitoring loop that must not stall the
 GPU on cudaMalloc/cudaFree's implicit synchronisation.  For them the library
 stages the pure state in a 1 MiB array fixed in its device image instead of a
 fresh buffer.  These tests call that entry point through the C ABI and check
-it against the allocating dmsim_pure_metrics, two calls in a row (the second
-call finds the array holding the first call's data), plus the size limit.
+it against the allocating dmsim_pure_metrics and against the same numbers
+computed on the host from the copied-back state (FP64 and complex64), two
+calls in a row (the second call finds the array holding the first call's
+data), plus the size limit.
 
 This file is collected last on purpose, and passes alone in a fresh process too.
 """
@@ -54,6 +56,40 @@ def test_noalloc_metrics_match_allocating_entry_point(engine, oracle):
                     assert st == engine.OK, engine.lib().dmsim_last_error(s._h)
                     assert close(got, want, 1e-12), (got, want)
             assert abs(want["trace"] - 1) < 1e-10
+
+
+def numpy_metrics(rho, psi):
+    """fidelity, trace, max |rho - psi psi^+|, ||rho - psi psi^+||_F on the host."""
+    d = rho - np.outer(psi, psi.conj())
+    return {"fidelity": float(np.real(psi.conj() @ rho @ psi)), "trace": float(np.real(np.trace(rho))),
+            "max_abs_err": float(np.abs(d).max()), "frob_err": float(np.linalg.norm(d))}
+
+
+@pytest.mark.parametrize("precision", ["fp64", "c64"])
+def test_noalloc_metrics_match_host_arithmetic(engine, oracle, precision):
+    """Independent of the device kernel the two entry points share: the same
+    four numbers computed on the host from the copied-back rho, for an FP64
+    and a complex64 state, two calls in a row."""
+    n = 7
+    circ = W.table_mix(n, 80, seed=93)
+    sr, si = oracle.sv_sim(n, circ)
+    psi = sr + 1j * si
+    psi_off = psi.copy()
+    psi_off[3] += 1e-3
+    with engine.Simulation(n, mode="fused", precision=precision) as s:
+        s.extend(circ)
+        s.upload()
+        s.run()
+        re, im = s.get_dm()
+        d = 1 << n
+        rho = (re + 1j * im).reshape(d, d).T  # the result layout is rho^T
+        tol = 1e-12 if precision == "fp64" else 1e-6
+        for ref_psi in (psi, psi_off):
+            want = numpy_metrics(rho, ref_psi)
+            for _ in range(2):
+                st, got = noalloc(engine, s, ref_psi)
+                assert st == engine.OK, engine.lib().dmsim_last_error(s._h)
+                assert close(got, want, tol), (got, want)
 
 
 def test_noalloc_rejects_states_beyond_its_scratch(engine):
