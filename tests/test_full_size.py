@@ -72,6 +72,32 @@ def test_u3_cx_ccx_17q_complex64(engine, oracle):
     assert abs(1 - m["trace"]) <= 1e-6, m
 
 
+def test_complex64_trace_distance_trend(engine, oracle):
+    """complex64 (FP32 state) against the FP64 statevector: the exact trace
+    distance (Hermitian eigensolve of sigma - psi psi^+) on the 17-qubit
+    circuit family at 1000 gates, 8 to 10 qubits.  FP32 rounding of the state
+    after every pass leaves full-rank noise whose trace norm grows like
+    sqrt(2^n): measured 6.9e-6, 9.7e-6, 1.34e-5, which extrapolates to ~1.6e-4
+    at 17 qubits."""
+    td = {}
+    for n in (8, 9, 10):
+        circ = W.u3_cx_ccx(n, 1000, seed=5)
+        sr, si = oracle.sv_sim(n, circ)
+        psi = sr + 1j * si
+        with engine.Simulation(n, mode="fused", precision="c64") as s:
+            s.extend(circ)
+            s.upload()
+            s.run()
+            re, im = s.get_dm()
+        d = 1 << n
+        diff = (re + 1j * im).reshape(d, d).T - np.outer(psi, psi.conj())
+        lam = np.linalg.eigvalsh(0.5 * (diff + diff.conj().T))
+        td[n] = 0.5 * float(np.abs(lam).sum())
+    for n, t in td.items():
+        assert t <= 1.5e-5 * 2.0 ** ((n - 10) / 2), td
+    assert 1.3 <= td[10] / td[8] <= 3.0, td  # ~sqrt(2) per qubit
+
+
 def test_complex64_renormalisation(engine, oracle):
     """After a complex64 run rho is Hermitian and has unit trace to FP32
     precision; without renormalisation the FP32 drift shows."""
