@@ -257,12 +257,15 @@ def extra_workload(args):
         # 4-10 layers; one graph-captured launch (work-queue kernel for the
         # narrow circuits, the engine's own kernels for the wide ones) vs
         # sequential plain runs (the reference's method, one circuit at a time)
-        sweep = W.hea_sweep(512, seed=4)
+        ncirc = args.sweep_circuits
+        sweep = W.hea_sweep(ncirc, seed=4, nmax=args.sweep_nmax)
+        out["sweep"] = {"circuits": ncirc, "qubits": [6, args.sweep_nmax]}
         b = E.Batch([n for n, _ in sweep], mode="fused", max_k=args.max_k)
         for c, (n, circ) in enumerate(sweep):
             b.extend(c, circ)
         b.upload()
-        out["autotune_best_ms"] = b.autotune()
+        if not args.no_autotune:
+            out["autotune_best_ms"] = b.autotune()
         for _ in range(args.warmup):
             b.run()
         clocks.start()
@@ -273,12 +276,13 @@ def extra_workload(args):
         out["clocks"] = clocks.stop()
         st = b.stats()
         out["batched_s"] = float(np.mean(ms)) / 1e3
-        out["batched_circuits_per_s"] = 512 / out["batched_s"]
+        out["batched_circuits_per_s"] = ncirc / out["batched_s"]
         out["batch_stats"] = st
         out["batched_GBps"] = st["bytes"] / (out["batched_s"]) / 1e9
-        for label, kw in (("sequential_plain_fp64", dict(mode="plain", plain_arith="fp64")),
-                          ("sequential_plain_df64", dict(mode="plain", plain_arith="df64")),
-                          ("sequential_fused_fp64", dict(mode="fused", fused_arith="fp64"))):
+        seq_arms = () if args.no_plain else (("sequential_plain_fp64", dict(mode="plain", plain_arith="fp64")),
+                                             ("sequential_plain_df64", dict(mode="plain", plain_arith="df64")),
+                                             ("sequential_fused_fp64", dict(mode="fused", fused_arith="fp64")))
+        for label, kw in seq_arms:
             seq = 0.0
             worst = 0.0
             for c, (n, circ) in enumerate(sweep):
@@ -385,6 +389,9 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-16q", action="store_true", help="skip the 16-qubit configuration")
+    ap.add_argument("--sweep-circuits", type=int, default=512, help="sweep workload: number of circuits")
+    ap.add_argument("--sweep-nmax", type=int, default=12, help="sweep workload: qubits uniform in {6..nmax}")
+    ap.add_argument("--no-autotune", action="store_true", help="sweep workload: the batch's default settings")
     ap.add_argument("--workload", default="table14",
                     help="table14 (the bench line), or extra measurements: sweep, qft16, c64_17, peaks")
     args = ap.parse_args()

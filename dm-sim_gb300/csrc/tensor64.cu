@@ -26,23 +26,25 @@
 // entries): the error of an output is below 2^-54 of its operator row's
 // 1-norm times its column's largest value, per step.
 //
-// Threads: 512 (16 warps), one block per SM.  Thread (warp w, lane l) owns
-// tile column m = 32 (w & 3) + l -- the TMEM lane its warp may read -- and
-// quarter q = w >> 2 of it: R/4 consecutive values (real parts for q < 2,
-// imaginary parts for q >= 2).  Thread 0 issues the MMAs; every thread
-// issues its share of the bulk copies.  Per tile:
-//   2. ket digits -> A_ket;  3. the ket MMAs (TMEM set t&1)
-//   4. the previous tile's bra accumulators -> FP64 -> global stores,
-//      overlapping the ket MMAs
-//   5. ket accumulators -> exact int64 outputs in the tile buffer
-//   6. bra digits -> A_bra; the next tile's values (TMA bulk copies of its
-//      runs, issued two tiles ahead) and their column maxima
-//   7. the bra MMAs (same set);  8. the loads two tiles ahead into the freed
-//      buffer.  The bra MMAs overlap the next tile's steps 2-3.
-// Three block barriers per tile (after steps 2, 5 and 6).  Every wait is
-// bounded; on expiry the block sets the error flag, waits (bounded) for its
-// own copies and MMAs in flight, releases its TMEM and returns, and the host
-// reports DMSIM_ERR_TIMEOUT.
+// Threads: 512 (16 warps), one block per SM, as two independent groups of 8
+// warps that take alternate tiles of the block, each with its own tile
+// buffer, digit operand, tensor-memory accumulator set, mbarriers and named
+// barrier: while one group waits at a barrier or on its products, the other
+// issues.  Thread (warp w, lane l) of a group owns tile column m = 32 (w & 3)
+// + l -- the TMEM lane its warp may read -- and half (w >> 2) & 1 of it: the
+// D real or the D imaginary parts.  The group's first thread issues its MMAs;
+// every thread issues its share of the group's bulk copies.  Per tile:
+//   1. wait for the tile (TMA bulk copies of its runs, issued one tile
+//      ahead), column maxima;  2. ket digits -> A;  3. the ket MMAs
+//   4. ket accumulators -> exact int64 outputs in place of the tile, bra
+//      magnitude keys;  5. bra digits -> A;  6. the bra MMAs, and the group's
+//      next tile loaded into the freed buffer;  7. bra accumulators -> FP64
+//      -> global stores.
+// Four group barriers per tile (after steps 1, 2, 4 and 5); the ones after
+// steps 1 and 4 also OR the threads' timeout flags.  Every wait is bounded; on
+// expiry the group leaves its loop at the next such barrier, waits (bounded)
+// for its own copies and MMAs in flight, sets the error flag, and the block
+// releases its TMEM; the host reports DMSIM_ERR_TIMEOUT.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -56,39 +58,43 @@ namespace dmg {
 namespace {
 
 constexpr int kT64Threads = 512;
+constexpr int kT64GroupThreads = 256;
 constexpr uint32_t kT64WaitPolls = 1u << 24;
 
 template <int K>
 struct T64 {
   static constexpr int D = 1 << K, R = 2 * D, G = 128 / D, TILE = 128 * D;
-  static constexpr int Q = R / 4;                          // values of one column per thread
   static constexpr uint32_t SBO = 16 * R;                  // bytes between 8-row groups of an R-wide operand
   static constexpr uint32_t A_BYTES = 128 * R * 2;         // one digit slice of the 128 columns
   static constexpr uint32_t B_BYTES = R * R * 2;           // one digit slice of W or V
-  static constexpr uint32_t SET_COLS = kTc64Orders * R;    // accumulators of one step
-  static constexpr uint32_t TMEM_COLS = 2 * SET_COLS;      // two sets: 512 (K = 4), 256 (K = 3)
+  static constexpr uint32_t SET_COLS = kTc64Orders * R;    // accumulators of one group
+  static constexpr uint32_t TMEM_COLS = 2 * SET_COLS;      // 512 (K = 4), 256 (K = 3)
   static constexpr uint32_t BUF_BYTES = TILE * 8 * 2;      // one tile, re + im, 8 bytes per real
   static_assert(TMEM_COLS <= 512, "two accumulator sets must fit in tensor memory");
+};
+
+template <int K>
+struct T64Group {
+  static constexpr int D = 1 << K;
+  uint64_t full;            // the group's tile loads
+  uint64_t mma;             // the group's ket and bra commits, alternating
+  uint32_t colmax[2][128];  // per half and column: largest FP64 exponent field
+  uint32_t brmax[128];      // per bra column: magnitude key of the ket outputs
+  int colEt[128 / D][D];    // biased exponent of ket column (b, f)'s grid, at [f][b]
 };
 
 template <int K>
 struct T64Tables {
   static constexpr int D = 1 << K;
   uint64_t hioff[256];
-  uint64_t full[2];       // tile loads into buffer 0 / 1
-  uint64_t mma[2];        // commits of the ket (0) and bra (1) products
-  uint32_t stmask[8];
-  int lk[D], lb[D];
-  int ew[2][D];
   // output (a, b) of a tile: bits 0..47 its offset from the tile base minus
   // the free bits, bits 48..55 the bra row exponent ew[1][b] + 128, bit 63
   // set when its run is stored
   uint64_t outoff[D][D];
-  uint32_t colmax[4][128];  // per quarter and column: largest FP64 exponent field
-  uint32_t brmax[2][128];   // per tile parity and bra column: magnitude key of the ket outputs
-  int colEt[128 / D][D];    // biased exponent of ket column (b, f)'s grid, at [f][b]
+  T64Group<K> grp[2];
+  int lk[D], lb[D];
+  int ew[2][D];
   uint32_t slot;
-  int abort_;
 };
 
 template <int K>
@@ -96,6 +102,21 @@ constexpr size_t t64_smem_bytes() {
   using S = T64<K>;
   return 2 * (size_t)kTc64Slices * S::A_BYTES + 2 * (size_t)kTc64Slices * S::B_BYTES + 2 * (size_t)S::BUF_BYTES +
          sizeof(T64Tables<K>);
+}
+
+// Named barrier of group g (ids 1, 2), and the same with an OR of p over the group.
+__device__ __forceinline__ void group_bar(int g) {
+  asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "n"(kT64GroupThreads) : "memory");
+}
+__device__ __forceinline__ bool group_bar_or(int g, bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred ip, op;\n\tsetp.ne.u32 ip, %1, 0;\n\tbar.red.or.pred op, %2, %3, ip;\n\t"
+      "selp.u32 %0, 1, 0, op;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)p), "r"(1 + g), "n"(kT64GroupThreads)
+      : "memory");
+  return r != 0;
 }
 
 __device__ __forceinline__ uint64_t shr_u64(uint64_t x, uint32_t s) {  // s >= 64 gives 0
@@ -231,20 +252,19 @@ __global__ void __launch_bounds__(kT64Threads, 1)
     k_pass_tc64(uint64_t* __restrict__ re, uint64_t* __restrict__ im, const TcDesc64<K>* __restrict__ dp,
                 int* __restrict__ err) {
   using S = T64<K>;
-  constexpr int D = S::D, R = S::R, G = S::G, Q = S::Q, TILE = S::TILE;
+  constexpr int D = S::D, R = S::R, G = S::G, TILE = S::TILE;
   extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char* sAk = smem;
-  unsigned char* sAb = sAk + kTc64Slices * S::A_BYTES;
-  unsigned char* sB = sAb + kTc64Slices * S::A_BYTES;  // W digits, then V digits
-  uint64_t* bufs = reinterpret_cast<uint64_t*>(sB + 2 * kTc64Slices * S::B_BYTES);  // [buffer][re, im][TILE]
+  unsigned char* sB = smem + 2 * kTc64Slices * S::A_BYTES;                          // W digits, then V digits
+  uint64_t* bufs = reinterpret_cast<uint64_t*>(sB + 2 * kTc64Slices * S::B_BYTES);  // [group][re, im][TILE]
   T64Tables<K>& tb = *reinterpret_cast<T64Tables<K>*>(bufs + 4 * TILE);
   const PassHeader& h = dp->h;
   const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
-  const int m = 32 * (w & 3) + l, q = w >> 2;
+  const int g = w >> 3, gtid = tid & (kT64GroupThreads - 1);
+  const int m = 32 * (w & 3) + l, half = (w >> 2) & 1;
   const int r = m / G, f = m & (G - 1);
-  const int c0 = q * Q;       // first value of this thread's quarter of a column
-  const int half = c0 / D;    // 0: real parts, 1: imaginary parts
-  const int cb = c0 % D;      // first ket (ket step) or bra (bra step) index of the quarter
+  unsigned char* sA = smem + g * kTc64Slices * S::A_BYTES;  // the group's digit operand (ket, then bra)
+  uint64_t* buf = bufs + (size_t)g * 2 * TILE;             // the group's tile, then its ket outputs
+  T64Group<K>& gp = tb.grp[g];
 
   // ---- per-pass tables, the operator's digits, tensor memory, barriers
   {
@@ -259,7 +279,6 @@ __global__ void __launch_bounds__(kT64Threads, 1)
     for (int j = 0; j < h.mhi; j++) off |= (uint64_t)((run >> j) & 1) << h.hipos[j];
     tb.hioff[run] = off;
   }
-  if (tid < 8) tb.stmask[tid] = h.stmask[tid];
   if (tid < D) {
     int lk = 0, lb = 0;
     for (int i = 0; i < K; i++) {
@@ -282,277 +301,225 @@ __global__ void __launch_bounds__(kT64Threads, 1)
     const uint64_t stored = (h.stmask[run >> 5] >> (run & 31)) & 1;
     tb.outoff[a][bb] = off | ((uint64_t)(dp->ew[1][bb] + 128) << 48) | (stored << 63);
   }
-  if (tid < 128) tb.brmax[0][tid] = tb.brmax[1][tid] = 0;
-  if (tid == 0) tb.abort_ = 0;
+  if (tid < 256) tb.grp[tid >> 7].brmax[tid & 127] = 0;
   if (w == 0) {
     tc::tmem_alloc(&tb.slot, S::TMEM_COLS);
     tc::tmem_relinquish();
   }
   if (tid == 0) {
-    tc::mbar_init(&tb.full[0], 1);
-    tc::mbar_init(&tb.full[1], 1);
-    tc::mbar_init(&tb.mma[0], 1);
-    tc::mbar_init(&tb.mma[1], 1);
+    for (int gi = 0; gi < 2; gi++) {
+      tc::mbar_init(&tb.grp[gi].full, 1);
+      tc::mbar_init(&tb.grp[gi].mma, 1);
+    }
     tc::mbar_fence_init();
   }
   tc::fence_proxy_async_smem();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  const uint32_t tmem = tb.slot;
+  const uint32_t tmem = tb.slot + (uint32_t)g * S::SET_COLS;  // the group's accumulator set
   const uint32_t tlane = (uint32_t)(32 * (w & 3)) << 16;
 
   int lf_g = 0;  // free-bit offset of this column's group f (the same in both steps)
   for (int j = 0; j < h.g; j++) lf_g |= ((f >> j) & 1) << h.freepos[j];
   const int L = h.L, runlen = 1 << L, ncopies = 2 << h.mhi;  // runs of the real and imaginary arrays
-  const uint64_t ntiles = h.ntiles, step = gridDim.x;
-  // this thread's values of the loaded tile (ket step): entries (a = cb + c, r, f) at basek + offk[c]
-  int offk[Q];
+  const uint64_t ntiles = h.ntiles, gstep = 2 * (uint64_t)gridDim.x;
+  // ket step: this thread's values (a, b = r, f), a = 0..D-1, of its half, at vals[posk[a]]
+  const uint64_t* vals = buf + (half ? TILE : 0);
+  int posk[D];
+  {
+    const int basek = tb.lb[r] + lf_g;
 #pragma unroll
-  for (int c = 0; c < Q; c++) offk[c] = tb.lk[cb + c];
-  const int basek = tb.lb[r] + lf_g;
-  // accumulators are read and digits written 4 values at a time
-  constexpr int QH = 4;
+    for (int a = 0; a < D; a++) posk[a] = basek + tb.lk[a];
+  }
   // The ket step's exact integer outputs replace the tile in its buffer, at
   // [half][a][b ^ (a & 1)][f]: the ket step writes, for one a, 32 consecutive
   // words per warp, and the bra step reads, for one b, columns a of both
   // parities -- both free of bank conflicts.
   auto yidx = [&](int a, int b) { return half * TILE + (a * D + (b ^ (a & 1))) * G + f; };
 
-  // Loads of a tile: thread 0 arms the buffer's barrier with the tile's bytes
-  // before a block barrier, after which every thread issues its share of the
-  // 1-D bulk copies (one per run of each array).
-  auto copy_tile = [&](uint64_t t, int b) {
-    uint64_t* dst = bufs + (size_t)b * 2 * TILE;
+  // Loads of a tile into the group's buffer: the group's first thread arms
+  // its barrier with the tile's bytes before a group barrier, after which
+  // every thread of the group issues its share of the 1-D bulk copies (one
+  // per run of each array).
+  auto copy_tile = [&](uint64_t t) {
     const uint64_t base = tile_base(h, t);
-    for (int i = tid; i < ncopies; i += kT64Threads) {
+    for (int i = gtid; i < ncopies; i += kT64GroupThreads) {
       const int run = i >> 1, arr = i & 1;
-      tc::bulk_g2s(dst + arr * TILE + run * runlen, (arr ? im : re) + base + tb.hioff[run], (uint32_t)runlen * 8u,
-                   &tb.full[b]);
+      tc::bulk_g2s(buf + arr * TILE + run * runlen, (arr ? im : re) + base + tb.hioff[run], (uint32_t)runlen * 8u,
+                   &gp.full);
     }
   };
 
-  // outstanding asynchronous work, the same on every thread
-  uint32_t phf0 = 0, phf1 = 0, phk = 0, phb = 0;
-  int pendf0 = 0, pendf1 = 0, pendk = 0, pendb = 0;
-  bool timed_out = false;
-  // a phase that did not complete stays pending (the teardown waits for it again)
+  // outstanding asynchronous work of this thread's view; a phase that did not
+  // complete stays pending (the teardown waits for it again)
+  uint32_t phf = 0, phm = 0;
+  int pendf = 0, pendm = 0;
+  bool bad = false;  // one of this thread's waits expired
   auto wait = [&](uint64_t* bar, uint32_t& ph, int& pend) {
     if (!tc::mbar_wait_bounded(bar, ph, kT64WaitPolls)) {
-      timed_out = true;
-      tb.abort_ = 1;
-      return;
+      bad = true;
+      return false;
     }
     ph ^= 1u;
     pend = 0;
-  };
-  auto wait_full = [&](int b) {
-    if (b) wait(&tb.full[1], phf1, pendf1);
-    else wait(&tb.full[0], phf0, pendf0);
+    return true;
   };
 
-  // the previous tile's bra outputs -> FP64 -> its stored runs
-  auto bra_out = [&](uint32_t set, uint64_t base, uint32_t mkey) {
-    const int pa = (int)mkey + tb.ew[0][r] - 1106 - 128;
-    uint64_t* arr = (half ? im : re) + base + lf_g;
-#pragma unroll
-    for (int c4 = 0; c4 < Q; c4 += QH) {
-      float sv[kTc64Orders][QH];
-      const uint32_t ta = tmem + tlane + set + c0 + c4;
-#pragma unroll
-      for (int o = 0; o < kTc64Orders; o++) tc::tmem_ld4(ta + o * R, sv[o]);
-      tc::tmem_wait_ld();
-#pragma unroll
-      for (int c = 0; c < QH; c++) {
-        const uint64_t T = tb.outoff[r][cb + c4 + c];
-        if (!(T >> 63)) continue;  // a run the pass does not change
-        const int64_t Y =
-            combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c], sv[6][c], sv[7][c]);
-        arr[T & 0xFFFFFFFFFFFFull] = to_fp64(Y, pa + (int)((T >> 48) & 0xFF));
-      }
-    }
-    tc::fence_before_sync();
-  };
-
-  // this thread's values of the tile in buffer b (ket step) and their largest exponent field
-  uint32_t xl[Q], xh[Q];
-  auto read_tile = [&](int b) {
-    const uint64_t* barr = bufs + (size_t)b * 2 * TILE + (half ? TILE : 0);
-    uint32_t emx = 0;
-#pragma unroll
-    for (int c = 0; c < Q; c++) {
-      const uint64_t v = barr[basek + offk[c]];
-      xl[c] = (uint32_t)v;
-      xh[c] = (uint32_t)(v >> 32);
-      emx = max(emx, xh[c] & 0x7FF00000u);
-    }
-    tb.colmax[q][m] = emx;
-  };
-
-  // ---- prologue: the first two tiles in flight, the first one's values
-  const uint64_t t0 = blockIdx.x;
-  if (tid == 0) {
-    if (t0 < ntiles) tc::mbar_arrive_expect_tx(&tb.full[0], S::BUF_BYTES);
-    if (t0 + step < ntiles) tc::mbar_arrive_expect_tx(&tb.full[1], S::BUF_BYTES);
+  // ---- prologue: the group's first tile in flight
+  uint64_t t = blockIdx.x + (uint64_t)g * gridDim.x;
+  if (gtid == 0 && t < ntiles) tc::mbar_arrive_expect_tx(&gp.full, S::BUF_BYTES);
+  group_bar(g);
+  if (t < ntiles) {
+    copy_tile(t);
+    pendf = 1;
   }
-  __syncthreads();
-  if (t0 < ntiles) copy_tile(t0, 0);
-  if (t0 + step < ntiles) copy_tile(t0 + step, 1);
-  pendf0 = t0 < ntiles;
-  pendf1 = t0 + step < ntiles;
-  if (t0 < ntiles) {
-    wait_full(0);
-    read_tile(0);
-  }
-  __syncthreads();
 
-  bool has_prev = false;
-  uint64_t prev_base = 0;
-  uint32_t prev_set = 0, prev_mkey = 0;
-  int it = 0;
-  for (uint64_t t = t0; t < ntiles; t += step, it++) {
-    if (tb.abort_) break;
-    const int b = it & 1;
-    const uint32_t set = (uint32_t)b * S::SET_COLS;
-    uint64_t* buf = bufs + (size_t)b * 2 * TILE;
-    const uint64_t tn = t + 2 * step;
-
-    // ---- 2: ket digits of column (b = r, f), from the values read before the last barrier
-    int Ec = 0;
+  for (; t < ntiles; t += gstep) {
+    // ---- 1: the tile's values and their column maxima
+    wait(&gp.full, phf, pendf);
     {
-      uint32_t ecm = max(max(tb.colmax[0][m], tb.colmax[1][m]), max(tb.colmax[2][m], tb.colmax[3][m]));
-      ecm = max(ecm, 64u << 20);
-      Ec = (int)(ecm >> 20);
-      if (q == 0) tb.colEt[f][r] = Ec;
-      uint32_t pk[Q / 2][kTc64Slices];
+      uint32_t emx = 0;
 #pragma unroll
-      for (int c2 = 0; c2 < Q / 2; c2++) {
+      for (int a = 0; a < D; a++) emx = max(emx, (uint32_t)(vals[posk[a]] >> 32) & 0x7FF00000u);
+      gp.colmax[half][m] = emx;
+    }
+    if (group_bar_or(g, bad)) break;
+
+    // ---- 2: ket digits of column (b = r, f) on its grid
+    uint32_t ecm = max(max(gp.colmax[0][m], gp.colmax[1][m]), 64u << 20);
+    const int Ec = (int)(ecm >> 20);
+    if (half == 0) gp.colEt[f][r] = Ec;
+#pragma unroll
+    for (int ch = 0; ch < D / 8; ch++) {
+      uint32_t pk[4][kTc64Slices];
+#pragma unroll
+      for (int c2 = 0; c2 < 4; c2++) {
         float d0[kTc64Slices], d1[kTc64Slices];
-        digits_fp64(xl[2 * c2], xh[2 * c2], ecm, d0);
-        digits_fp64(xl[2 * c2 + 1], xh[2 * c2 + 1], ecm, d1);
+        const uint64_t v0 = vals[posk[8 * ch + 2 * c2]], v1 = vals[posk[8 * ch + 2 * c2 + 1]];
+        digits_fp64((uint32_t)v0, (uint32_t)(v0 >> 32), ecm, d0);
+        digits_fp64((uint32_t)v1, (uint32_t)(v1 >> 32), ecm, d1);
 #pragma unroll
         for (int j = 0; j < kTc64Slices; j++) pk[c2][j] = pack_bf16x2(d0[j], d1[j]);
       }
-      store_packed<Q>(sAk, S::A_BYTES, tc_kmajor_offset(m, c0, S::SBO), pk);
-      tc::fence_proxy_async_smem();
+      store_packed<8>(sA, S::A_BYTES, tc_kmajor_offset(m, half * D + 8 * ch, S::SBO), pk);
     }
+    tc::fence_proxy_async_smem();
     tc::fence_before_sync();
-    __syncthreads();
+    group_bar(g);
     tc::fence_after_sync();
 
     // ---- 3: ket products
-    if (tid == 0) {
-      issue_step<K>(sAk, sB, tmem + set);
-      tc::mma_commit(&tb.mma[0]);
+    if (gtid == 0) {
+      issue_step<K>(sA, sB, tmem);
+      tc::mma_commit(&gp.mma);
     }
-    {
-      pendk = 1;
-      // ---- 4: the previous tile's outputs (overlapping the ket products)
-      if (has_prev) {
-        wait(&tb.mma[1], phb, pendb);
-        tc::fence_after_sync();
-        if (!timed_out) bra_out(prev_set, prev_base, prev_mkey);
-      }
-      // ---- 5: ket outputs -> exact integers (in place of the tile), and the
-      // bra columns' magnitude keys: Ec + exponent of |S_0| + |S_1|/256 + 65,
-      // which bounds |Y| 2^Ec by 2^(key - 86) (1 + 2^-23)
-      wait(&tb.mma[0], phk, pendk);
+    pendm = 1;
+
+    // ---- 4: ket outputs -> exact integers (in place of the tile), and the
+    // bra columns' magnitude keys: Ec + exponent of |S_0| + |S_1|/256 + 65,
+    // which bounds |Y| 2^Ec by 2^(key - 86) (1 + 2^-23)
+    if (wait(&gp.mma, phm, pendm)) {
       tc::fence_after_sync();
-      if (!timed_out) {
 #pragma unroll
-        for (int c4 = 0; c4 < Q; c4 += QH) {
-          float sv[kTc64Orders][QH];
-          const uint32_t ta = tmem + tlane + set + c0 + c4;
+      for (int c4 = 0; c4 < D; c4 += 4) {
+        float sv[kTc64Orders][4];
+        const uint32_t ta = tmem + tlane + half * D + c4;
 #pragma unroll
-          for (int o = 0; o < kTc64Orders; o++) tc::tmem_ld4(ta + o * R, sv[o]);
-          tc::tmem_wait_ld();
+        for (int o = 0; o < kTc64Orders; o++) tc::tmem_ld4(ta + o * R, sv[o]);
+        tc::tmem_wait_ld();
 #pragma unroll
-          for (int c = 0; c < QH; c++) {
-            const int a = cb + c4 + c;
-            buf[yidx(a, r)] = (uint64_t)combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c],
-                                                       sv[6][c], sv[7][c]);
-            const float mag = fmaf(fabsf(sv[1][c]), 0.00390625f, fabsf(sv[0][c])) + 65.0f;
-            atomicMax(&tb.brmax[b][a * G + f], (uint32_t)Ec + (__float_as_uint(mag) >> 23));
-          }
+        for (int c = 0; c < 4; c++) {
+          const int a = c4 + c;
+          buf[yidx(a, r)] = (uint64_t)combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c],
+                                                     sv[6][c], sv[7][c]);
+          const float mag = fmaf(fabsf(sv[1][c]), 0.00390625f, fabsf(sv[0][c])) + 65.0f;
+          atomicMax(&gp.brmax[a * G + f], (uint32_t)Ec + (__float_as_uint(mag) >> 23));
         }
       }
     }
     tc::fence_before_sync();
-    __syncthreads();
-    if (tb.abort_) break;
+    if (group_bar_or(g, bad)) break;
     tc::fence_after_sync();
 
-    // ---- 6: bra digits of column (a = r, f): values Y_b 2^Ec(b) on the grid
+    // ---- 5: bra digits of column (a = r, f): values Y_b 2^Ec(b) on the grid
     // 2^(mkey - 141), |v| < 2^55 (1 + 2^-23)
-    const uint32_t mkey = tb.brmax[b][m];
-    {
-      int ecol[Q];
+    const uint32_t mkey = gp.brmax[m];
 #pragma unroll
-      for (int c = 0; c < Q; c++) ecol[c] = tb.colEt[f][cb + c];
-      uint32_t pk[Q / 2][kTc64Slices];
+    for (int ch = 0; ch < D / 8; ch++) {
+      uint32_t pk[4][kTc64Slices];
 #pragma unroll
-      for (int c2 = 0; c2 < Q / 2; c2++) {
+      for (int c2 = 0; c2 < 4; c2++) {
         float d[2][kTc64Slices];
 #pragma unroll
         for (int u = 0; u < 2; u++) {
-          const int c = 2 * c2 + u;
-          const int64_t Y = (int64_t)buf[yidx(r, cb + c)];
-          const int sh = (int)mkey - 141 - ecol[c];
+          const int b = 8 * ch + 2 * c2 + u;
+          const int64_t Y = (int64_t)buf[yidx(r, b)];
+          const int sh = (int)mkey - 141 - gp.colEt[f][b];
           const int64_t v = sh >= 0 ? shr_s64(Y, (uint32_t)sh) : shl_s64(Y, (uint32_t)(-sh));
           digits_int(v, d[u]);
         }
 #pragma unroll
         for (int j = 0; j < kTc64Slices; j++) pk[c2][j] = pack_bf16x2(d[0][j], d[1][j]);
       }
-      store_packed<Q>(sAb, S::A_BYTES, tc_kmajor_offset(m, c0, S::SBO), pk);
-      // the next tile's values (its loads were issued two tiles ago)
-      if (t + step < ntiles) {
-        wait_full(b ^ 1);
-        read_tile(b ^ 1);
-      }
-      if (tid < 128) tb.brmax[b ^ 1][tid] = 0;  // the next tile's magnitude keys
-      if (tid == 0 && tn < ntiles) tc::mbar_arrive_expect_tx(&tb.full[b], S::BUF_BYTES);  // this buffer's next loads
-      tc::fence_proxy_async_smem();
+      store_packed<8>(sA, S::A_BYTES, tc_kmajor_offset(m, half * D + 8 * ch, S::SBO), pk);
     }
+    const uint64_t tn = t + gstep;
+    if (gtid == 0 && tn < ntiles) tc::mbar_arrive_expect_tx(&gp.full, S::BUF_BYTES);  // the group's next tile
+    tc::fence_proxy_async_smem();
     tc::fence_before_sync();
-    __syncthreads();
+    group_bar(g);
     tc::fence_after_sync();
 
-    // ---- 7: bra products; 8: the loads two tiles ahead into this buffer
-    if (tid == 0) {
-      issue_step<K>(sAb, sB + kTc64Slices * S::B_BYTES, tmem + set);
-      tc::mma_commit(&tb.mma[1]);
+    // ---- 6: bra products; the group's next tile into the freed buffer
+    if (gtid == 0) {
+      issue_step<K>(sA, sB + kTc64Slices * S::B_BYTES, tmem);
+      tc::mma_commit(&gp.mma);
     }
-    pendb = 1;
+    pendm = 1;
+    if (gtid < 128) gp.brmax[gtid] = 0;  // the next tile's magnitude keys
     if (tn < ntiles) {
-      copy_tile(tn, b);
-      if (b) pendf1 = 1;
-      else pendf0 = 1;
+      copy_tile(tn);
+      pendf = 1;
     }
-    has_prev = true;
-    prev_base = tile_base(h, t);
-    prev_set = set;
-    prev_mkey = mkey;
+
+    // ---- 7: bra outputs -> FP64 -> the tile's stored runs
+    if (wait(&gp.mma, phm, pendm)) {
+      tc::fence_after_sync();
+      const int pa = (int)mkey + tb.ew[0][r] - 1106 - 128;
+      uint64_t* arr = (half ? im : re) + tile_base(h, t) + lf_g;
+#pragma unroll
+      for (int c4 = 0; c4 < D; c4 += 4) {
+        float sv[kTc64Orders][4];
+        const uint32_t ta = tmem + tlane + half * D + c4;
+#pragma unroll
+        for (int o = 0; o < kTc64Orders; o++) tc::tmem_ld4(ta + o * R, sv[o]);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const uint64_t T = tb.outoff[r][c4 + c];
+          if (!(T >> 63)) continue;  // a run the pass does not change
+          const int64_t Y =
+              combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c], sv[6][c], sv[7][c]);
+          arr[T & 0xFFFFFFFFFFFFull] = to_fp64(Y, pa + (int)((T >> 48) & 0xFF));
+        }
+      }
+    }
+    tc::fence_before_sync();  // the next tile's first barrier orders these reads before its MMAs
   }
-  if (has_prev && !tb.abort_) {
-    wait(&tb.mma[1], phb, pendb);
-    tc::fence_after_sync();
-    if (!timed_out) bra_out(prev_set, prev_base, prev_mkey);
-  }
-  // ---- teardown: nothing of this block may still be in flight when its
-  // tensor memory and shared memory are released (bounded, after an expiry)
-  __syncthreads();
-  if (tb.abort_) {
-    if (pendk) tc::mbar_wait_bounded(&tb.mma[0], phk, kT64WaitPolls << 2);
-    if (pendb) tc::mbar_wait_bounded(&tb.mma[1], phb, kT64WaitPolls << 2);
-    if (pendf0) tc::mbar_wait_bounded(&tb.full[0], phf0, kT64WaitPolls << 2);
-    if (pendf1) tc::mbar_wait_bounded(&tb.full[1], phf1, kT64WaitPolls << 2);
-    if (tid == 0) atomicExch(err, 1);
+
+  // ---- teardown: nothing of this group may still be in flight when the
+  // block's tensor memory and shared memory are released (bounded, after an
+  // expiry)
+  if (group_bar_or(g, bad)) {
+    if (pendm) tc::mbar_wait_bounded(&gp.mma, phm, kT64WaitPolls << 2);
+    if (pendf) tc::mbar_wait_bounded(&gp.full, phf, kT64WaitPolls << 2);
+    if (gtid == 0) atomicExch(err, 1);
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (w == 0) tc::tmem_dealloc(tmem, S::TMEM_COLS);
+  if (w == 0) tc::tmem_dealloc(tb.slot, S::TMEM_COLS);
 }
 
 template <int K>
