@@ -335,7 +335,7 @@ def extra_workload(args):
             plain.close()
         fused.close()
     elif args.workload == "c64_17":
-        n = 17
+        n = args.c64_n
         circ = W.u3_cx_ccx(n, 1000, seed=5)
         tensor = "all" if args.tensor == "all" else int(args.tensor)
         s = E.Simulation(n, mode="fused", max_k=args.max_k, precision="c64", planner=args.planner, tensor=tensor)
@@ -352,12 +352,13 @@ def extra_workload(args):
         out["trace_fp64_sum"] = float(d.sum())
         s.close()
         # the same circuit truncated to its first 16 qubits: complex64 against FP64
-        trunc = [g for g in circ if max(g[1]) < 16]
-        a = E.Simulation(16, mode="fused", max_k=args.max_k, precision="c64")
+        nt = min(n, 16)
+        trunc = [g for g in circ if max(g[1]) < nt]
+        a = E.Simulation(nt, mode="fused", max_k=args.max_k, precision="c64")
         a.extend(trunc)
         a.upload()
         a.run()
-        bsim = E.Simulation(16, mode="fused", max_k=args.max_k)
+        bsim = E.Simulation(nt, mode="fused", max_k=args.max_k)
         bsim.extend(trunc)
         bsim.upload()
         bsim.run()
@@ -392,6 +393,7 @@ def main():
     ap.add_argument("--sweep-circuits", type=int, default=512, help="sweep workload: number of circuits")
     ap.add_argument("--sweep-nmax", type=int, default=12, help="sweep workload: qubits uniform in {6..nmax}")
     ap.add_argument("--no-autotune", action="store_true", help="sweep workload: the batch's default settings")
+    ap.add_argument("--c64-n", type=int, default=17, help="c64_17 workload: qubits")
     ap.add_argument("--workload", default="table14",
                     help="table14 (the bench line), or extra measurements: sweep, qft16, c64_17, peaks")
     args = ap.parse_args()

@@ -169,6 +169,48 @@ __device__ __forceinline__ int pext_local(int loc, const int* lpos) {
   return a;
 }
 
+// Shared-memory layout of a tile: entry e sits at tile_sw(e) = e ^ ((e >> B)
+// & (E - 1)), E = 128 / sizeof(T) entries per 128-byte row of banks, B =
+// log2 E -- within its row, the entry's bank is XORed with its row's low
+// bits.  A column or row of an operator's targets (entries 2^p apart, p >= B)
+// then spreads over distinct banks instead of one, and runs of consecutive
+// entries stay conflict-free.  tile_sw is linear over GF(2): the offset of a
+// sum of disjoint bit fields is the XOR of the fields' offsets, so the ket,
+// bra and free offsets are swizzled once and combined with XOR.
+template <typename T>
+__device__ __forceinline__ int tile_sw(int e) {
+  constexpr int E = 128 / (int)sizeof(T);
+  constexpr int B = E == 32 ? 5 : 4;
+  return e ^ ((e >> B) & (E - 1));
+}
+// The pair of entries (e, e + 1), e even: one aligned vector slot, the two
+// entries in swapped order when the XOR mask is odd.
+template <typename T>
+__device__ __forceinline__ void st_pair(T* s, int e, typename Vec2<T>::type v) {
+  constexpr int E = 128 / (int)sizeof(T);
+  constexpr int B = E == 32 ? 5 : 4;
+  const int x = (e >> B) & (E - 1);
+  if (x & 1) {
+    const T t = v.x;
+    v.x = v.y;
+    v.y = t;
+  }
+  *reinterpret_cast<typename Vec2<T>::type*>(s + (e ^ (x & ~1))) = v;
+}
+template <typename T>
+__device__ __forceinline__ typename Vec2<T>::type ld_pair(const T* s, int e) {
+  constexpr int E = 128 / (int)sizeof(T);
+  constexpr int B = E == 32 ? 5 : 4;
+  const int x = (e >> B) & (E - 1);
+  typename Vec2<T>::type v = *reinterpret_cast<const typename Vec2<T>::type*>(s + (e ^ (x & ~1)));
+  if (x & 1) {
+    const T t = v.x;
+    v.x = v.y;
+    v.y = t;
+  }
+  return v;
+}
+
 // Per-pass constant tables, staged in shared memory once per block (or once
 // per work-queue range).  Arrays a class does not use shrink to one element.
 template <typename T, int K, int CLS_>
@@ -178,7 +220,7 @@ struct PassTables {
   static constexpr bool kMat = CLS == CLS_DENSE || CLS == CLS_SPARSE;
   uint64_t hioff[256];
   uint32_t ldmask[8], stmask[8];
-  int lk[D], lb[D];
+  int lk[D], lb[D];  // swizzled shared-memory offsets (tile_sw) of the ket / bra indices
   int lket[4], lbra[4];
   T ure[kMat ? D * D : 1], uim[kMat ? D * D : 1], vre[kMat ? D * D : 1], vim[kMat ? D * D : 1];
   T fre[CLS == CLS_PHASE ? D * D : 1], fim[CLS == CLS_PHASE ? D * D : 1];
@@ -222,8 +264,8 @@ __device__ void load_tables(const PassDesc<K>* __restrict__ dp, PassTables<T, K,
       lk |= ((tid >> i) & 1) << h.lket[i];
       lb |= ((tid >> i) & 1) << h.lbra[i];
     }
-    tb.lk[tid] = lk;
-    tb.lb[tid] = lb;
+    tb.lk[tid] = tile_sw<T>(lk);
+    tb.lb[tid] = tile_sw<T>(lb);
     tb.src[tid] = dp->op.src[tid];
     tb.srcb[tid] = dp->op.srcb[tid];
     tb.nnz[tid] = dp->op.nnz[tid];
@@ -306,8 +348,8 @@ __device__ __forceinline__ void regs_to_smem(const PassHeader& h, const PassTabl
     const int e = (threadIdx.x + k * kThreads) << 1;
     const int run = e >> h.L;
     if ((tb.ldmask[run >> 5] >> (run & 31)) & 1) {
-      *reinterpret_cast<T2*>(sre + e) = x.r[k];
-      *reinterpret_cast<T2*>(sim + e) = x.i[k];
+      st_pair<T>(sre, e, x.r[k]);
+      st_pair<T>(sim, e, x.i[k]);
     }
   }
 }
@@ -337,8 +379,8 @@ __device__ void run_tile(T* __restrict__ re, T* __restrict__ im, const PassHeade
     const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
     const T2 vr = ld2<T>(re + ga);
     const T2 vi = ld2<T>(im + ga);
-    *reinterpret_cast<T2*>(sre + e) = vr;
-    *reinterpret_cast<T2*>(sim + e) = vi;
+    st_pair<T>(sre, e, vr);
+    st_pair<T>(sim, e, vi);
   }
   __syncthreads();
   tile_body<T, K, CLS>(re, im, h, tb, base, sre, sim, free_offset(h));
@@ -370,6 +412,7 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
   const int runlen = 1 << L;
   const bool has_item = tid < G * D;
   const int r_item = tid >> g;  // b in the ket step, a in the bra step
+  const int slf = tile_sw<T>(lf);
 
   if constexpr (CLS == CLS_SUPER && K <= 2) {
     // ---- channel: each group's 4^K entries (a, b) <- S (4^K x 4^K), one thread per group
@@ -377,10 +420,11 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
     if (tid < G) {
       int ls = 0;
       for (int j = 0; j < g; j++) ls |= ((tid >> j) & 1) << h.freepos[j];
+      ls = tile_sw<T>(ls);
       T xr[DD], xi[DD];
 #pragma unroll
       for (int ab = 0; ab < DD; ab++) {
-        const int loc = ls + tb.lk[ab / D] + tb.lb[ab % D];
+        const int loc = ls ^ tb.lk[ab / D] ^ tb.lb[ab % D];
         xr[ab] = sre[loc];
         xi[ab] = sim[loc];
       }
@@ -395,7 +439,7 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
           ai = madd(mr, xi[j], ai);
           ai = madd(mi, xr[j], ai);
         }
-        const int loc = ls + tb.lk[o / D] + tb.lb[o % D];
+        const int loc = ls ^ tb.lk[o / D] ^ tb.lb[o % D];
         sre[loc] = ar;
         sim[loc] = ai;
       }
@@ -405,16 +449,16 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
       const int e = e2 << 1;
       const int run = e >> L;
       const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
-      st2<T>(re + ga, *reinterpret_cast<const T2*>(sre + e));
-      st2<T>(im + ga, *reinterpret_cast<const T2*>(sim + e));
+      st2<T>(re + ga, ld_pair<T>(sre, e));
+      st2<T>(im + ga, ld_pair<T>(sim, e));
     }
   } else if (CLS == CLS_DENSE || CLS == CLS_SPARSE || CLS == CLS_RLIN) {
     // ---- ket step: column (., b, f) <- U column
     if (has_item) {
       const int b = r_item;
-      const int cb = lf + tb.lb[b];
+      const int cb = slf ^ tb.lb[b];
       if (CLS == CLS_RLIN) {
-        const int p0 = cb + tb.lk[0], p1 = cb + tb.lk[1];
+        const int p0 = cb ^ tb.lk[0], p1 = cb ^ tb.lk[1];
         const T v[4] = {sre[p0], sim[p0], sre[p1], sim[p1]};
         T o[4];
 #pragma unroll
@@ -425,8 +469,8 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
         T xr[D], xi[D];
 #pragma unroll
         for (int c = 0; c < D; c++) {
-          xr[c] = sre[cb + tb.lk[c]];
-          xi[c] = sim[cb + tb.lk[c]];
+          xr[c] = sre[cb ^ tb.lk[c]];
+          xi[c] = sim[cb ^ tb.lk[c]];
         }
 #pragma unroll
         for (int a = 0; a < D; a++) {
@@ -442,8 +486,8 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
               ai.mad(ui, xr[c]);
             }
           }
-          sre[cb + tb.lk[a]] = ar.get();
-          sim[cb + tb.lk[a]] = ai.get();
+          sre[cb ^ tb.lk[a]] = ar.get();
+          sim[cb ^ tb.lk[a]] = ai.get();
         }
       } else {  // SPARSE: the rows advance together (2^K independent chains)
         Acc<T> yr[D], yi[D];
@@ -453,7 +497,7 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
             if (j < tb.nnz[a]) {
               const int c = tb.col[a * D + j];
               const T ur = tb.ure[a * D + c];
-              const T vr = sre[cb + tb.lk[c]], vi = sim[cb + tb.lk[c]];
+              const T vr = sre[cb ^ tb.lk[c]], vi = sim[cb ^ tb.lk[c]];
               yr[a].mad(ur, vr);
               yi[a].mad(ur, vi);
               if constexpr (!RE) {
@@ -466,8 +510,8 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
         }
 #pragma unroll
         for (int a = 0; a < D; a++) {
-          sre[cb + tb.lk[a]] = yr[a].get();
-          sim[cb + tb.lk[a]] = yi[a].get();
+          sre[cb ^ tb.lk[a]] = yr[a].get();
+          sim[cb ^ tb.lk[a]] = yi[a].get();
         }
       }
     }
@@ -475,9 +519,9 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
     // ---- bra step: row (a, ., f) <- V row (V = conj(U) for a superoperator pass)
     if (has_item) {
       const int a = r_item;
-      const int ca = lf + tb.lk[a];
+      const int ca = slf ^ tb.lk[a];
       if (CLS == CLS_RLIN) {
-        const int p0 = ca + tb.lb[0], p1 = ca + tb.lb[1];
+        const int p0 = ca ^ tb.lb[0], p1 = ca ^ tb.lb[1];
         const T v[4] = {sre[p0], sim[p0], sre[p1], sim[p1]};
         T o[4];
 #pragma unroll
@@ -489,8 +533,8 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
         T xr[D], xi[D];
 #pragma unroll
         for (int c = 0; c < D; c++) {
-          xr[c] = sre[ca + tb.lb[c]];
-          xi[c] = sim[ca + tb.lb[c]];
+          xr[c] = sre[ca ^ tb.lb[c]];
+          xi[c] = sim[ca ^ tb.lb[c]];
         }
 #pragma unroll
         for (int b = 0; b < D; b++) {
@@ -506,8 +550,8 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
               ai.mad(vi, xr[c]);
             }
           }
-          sre[ca + tb.lb[b]] = ar.get();
-          sim[ca + tb.lb[b]] = ai.get();
+          sre[ca ^ tb.lb[b]] = ar.get();
+          sim[ca ^ tb.lb[b]] = ai.get();
         }
       } else {  // SPARSE: the rows advance together (2^K independent chains)
         Acc<T> yr[D], yi[D];
@@ -517,7 +561,7 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
             if (j < tb.nnzb[b]) {
               const int c = tb.colb[b * D + j];
               const T mr = tb.vre[b * D + c];
-              const T vr = sre[ca + tb.lb[c]], vi = sim[ca + tb.lb[c]];
+              const T vr = sre[ca ^ tb.lb[c]], vi = sim[ca ^ tb.lb[c]];
               yr[b].mad(mr, vr);
               yi[b].mad(mr, vi);
               if constexpr (!RE) {
@@ -530,8 +574,8 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
         }
 #pragma unroll
         for (int b = 0; b < D; b++) {
-          sre[ca + tb.lb[b]] = yr[b].get();
-          sim[ca + tb.lb[b]] = yi[b].get();
+          sre[ca ^ tb.lb[b]] = yr[b].get();
+          sim[ca ^ tb.lb[b]] = yi[b].get();
         }
       }
     }
@@ -542,8 +586,8 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
       const int run = e >> L;
       if (!((tb.stmask[run >> 5] >> (run & 31)) & 1)) continue;
       const uint64_t ga = base + tb.hioff[run] + (uint64_t)(e & (runlen - 1));
-      st2<T>(re + ga, *reinterpret_cast<const T2*>(sre + e));
-      st2<T>(im + ga, *reinterpret_cast<const T2*>(sim + e));
+      st2<T>(re + ga, ld_pair<T>(sre, e));
+      st2<T>(im + ga, ld_pair<T>(sim, e));
     }
   } else {
     // ---- monomial: out[a][b] = f[a][b] * in[src[a]][srcb[b]], fused into the store
@@ -558,7 +602,7 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
         const int a = pext_local<K>(loc, tb.lket);
         const int b = pext_local<K>(loc, tb.lbra);
         const int sa = tb.src[a], sb = tb.srcb[b];
-        const int sl = loc - tb.lk[a] - tb.lb[b] + tb.lk[sa] + tb.lb[sb];
+        const int sl = tile_sw<T>(loc) ^ tb.lk[a] ^ tb.lb[b] ^ tb.lk[sa] ^ tb.lb[sb];
         const T vr = sre[sl], vi = sim[sl];
         if (CLS == CLS_MOVE) {
           outr[u] = vr;

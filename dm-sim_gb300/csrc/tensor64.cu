@@ -64,36 +64,50 @@ constexpr uint32_t kT64WaitPolls = 1u << 24;
 template <int K>
 struct T64 {
   static constexpr int D = 1 << K, R = 2 * D, G = 128 / D, TILE = 128 * D;
+  // entries from a loaded tile's real array to its imaginary array: 16-entry
+  // pieces 18 entries apart, and an offset of 8 pieces' banks between the two
+  static constexpr int ASTR = TILE / 16 * 18 + 8;
   static constexpr uint32_t SBO = 16 * R;                  // bytes between 8-row groups of an R-wide operand
   static constexpr uint32_t A_BYTES = 128 * R * 2;         // one digit slice of the 128 columns
   static constexpr uint32_t B_BYTES = R * R * 2;           // one digit slice of W or V
   static constexpr uint32_t SET_COLS = kTc64Orders * R;    // accumulators of one group
   static constexpr uint32_t TMEM_COLS = 2 * SET_COLS;      // 512 (K = 4), 256 (K = 3)
-  static constexpr uint32_t BUF_BYTES = TILE * 8 * 2;      // one tile, re + im, 8 bytes per real
+  static constexpr uint32_t TX_BYTES = TILE * 8 * 2;       // one tile, re + im, 8 bytes per real
+  static constexpr uint32_t BUF_BYTES = 2 * ASTR * 8;      // one group's tile buffer
   static_assert(TMEM_COLS <= 512, "two accumulator sets must fit in tensor memory");
+  static_assert(ASTR % 2 == 0 && BUF_BYTES % 16 == 0, "bulk copies need 16-byte aligned destinations");
 };
+
+// Layout of a loaded tile in shared memory: local entry e at piece_off(e),
+// 16-entry pieces (128 bytes, one bulk copy each) 18 entries apart, so that
+// the pieces' banks rotate by two 8-byte words per piece.  Each thread of the
+// ket step reads one column of the operator's targets (entries whose indices
+// differ in the target bits); with the pieces rotated, the columns a warp
+// reads at once fall into different banks even when the targets are the low
+// bits.  piece_off is additive over disjoint bit fields.
+__device__ __forceinline__ int piece_off(int e) { return e + 2 * (e >> 4); }
 
 template <int K>
 struct T64Group {
   static constexpr int D = 1 << K;
-  uint64_t full;            // the group's tile loads
-  uint64_t mma;             // the group's ket and bra commits, alternating
-  uint32_t colmax[2][128];  // per half and column: largest FP64 exponent field
-  uint32_t brmax[128];      // per bra column: magnitude key of the ket outputs
-  int colEt[128 / D][D];    // biased exponent of ket column (b, f)'s grid, at [f][b]
+  uint64_t full;          // the group's tile loads
+  uint64_t mma;           // the group's ket and bra commits, alternating
+  uint32_t brmax[128];    // per bra column: magnitude key of the ket outputs
+  int colEt[D][128 / D];  // biased exponent of ket column (b, f)'s grid, at [b][f]
 };
 
 template <int K>
 struct T64Tables {
   static constexpr int D = 1 << K;
   uint64_t hioff[256];
-  // output (a, b) of a tile: bits 0..47 its offset from the tile base minus
-  // the free bits, bits 48..55 the bra row exponent ew[1][b] + 128, bit 63
-  // set when its run is stored
+  // output (a, b) of a tile, at [b][a]: bits 0..47 its offset from the tile
+  // base minus the free bits, bits 48..55 the bra row exponent ew[1][b] +
+  // 128, bit 63 set when its run is stored
   uint64_t outoff[D][D];
   T64Group<K> grp[2];
-  int lk[D], lb[D];
+  int pk[D], pb[D];  // piece_off of the ket / bra index bits
   int ew[2][D];
+  int hipos[8];
   uint32_t slot;
 };
 
@@ -252,18 +266,24 @@ __global__ void __launch_bounds__(kT64Threads, 1)
     k_pass_tc64(uint64_t* __restrict__ re, uint64_t* __restrict__ im, const TcDesc64<K>* __restrict__ dp,
                 int* __restrict__ err) {
   using S = T64<K>;
-  constexpr int D = S::D, R = S::R, G = S::G, TILE = S::TILE;
+  constexpr int D = S::D, R = S::R, G = S::G, TILE = S::TILE, ASTR = S::ASTR;
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* sB = smem + 2 * kTc64Slices * S::A_BYTES;                          // W digits, then V digits
-  uint64_t* bufs = reinterpret_cast<uint64_t*>(sB + 2 * kTc64Slices * S::B_BYTES);  // [group][re, im][TILE]
-  T64Tables<K>& tb = *reinterpret_cast<T64Tables<K>*>(bufs + 4 * TILE);
+  uint64_t* bufs = reinterpret_cast<uint64_t*>(sB + 2 * kTc64Slices * S::B_BYTES);  // [group][re, im][ASTR]
+  T64Tables<K>& tb = *reinterpret_cast<T64Tables<K>*>(bufs + 4 * ASTR);
   const PassHeader& h = dp->h;
   const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
   const int g = w >> 3, gtid = tid & (kT64GroupThreads - 1);
+  // digit steps: column mc = 16 (w & 7) + (l & 15), half hc = l >> 4 (both
+  // halves of a column in one warp)
+  const int mc = 16 * (w & 7) + (l & 15), hc = l >> 4;
+  const int rc = mc / G, fc = mc & (G - 1);
+  // accumulator steps: column m = 32 (w & 3) + l -- the TMEM lane its warp
+  // may read -- half (w >> 2) & 1
   const int m = 32 * (w & 3) + l, half = (w >> 2) & 1;
   const int r = m / G, f = m & (G - 1);
   unsigned char* sA = smem + g * kTc64Slices * S::A_BYTES;  // the group's digit operand (ket, then bra)
-  uint64_t* buf = bufs + (size_t)g * 2 * TILE;             // the group's tile, then its ket outputs
+  uint64_t* buf = bufs + (size_t)g * 2 * ASTR;             // the group's tile, then its ket outputs
   T64Group<K>& gp = tb.grp[g];
 
   // ---- per-pass tables, the operator's digits, tensor memory, barriers
@@ -274,9 +294,10 @@ __global__ void __launch_bounds__(kT64Threads, 1)
       reinterpret_cast<uint4*>(sB)[i] = reinterpret_cast<const uint4*>(&dp->sl[side][0][0])[rest];
     }
   }
-  for (int run = tid; run < (1 << h.mhi); run += blockDim.x) {
+  const int mhi = h.mhi, L = h.L;
+  for (int run = tid; run < (1 << mhi); run += blockDim.x) {
     uint64_t off = 0;
-    for (int j = 0; j < h.mhi; j++) off |= (uint64_t)((run >> j) & 1) << h.hipos[j];
+    for (int j = 0; j < mhi; j++) off |= (uint64_t)((run >> j) & 1) << h.hipos[j];
     tb.hioff[run] = off;
   }
   if (tid < D) {
@@ -285,8 +306,8 @@ __global__ void __launch_bounds__(kT64Threads, 1)
       lk |= ((tid >> i) & 1) << h.lket[i];
       lb |= ((tid >> i) & 1) << h.lbra[i];
     }
-    tb.lk[tid] = lk;
-    tb.lb[tid] = lb;
+    tb.pk[tid] = piece_off(lk);
+    tb.pb[tid] = piece_off(lb);
     tb.ew[0][tid] = dp->ew[0][tid];
     tb.ew[1][tid] = dp->ew[1][tid];
   }
@@ -294,13 +315,14 @@ __global__ void __launch_bounds__(kT64Threads, 1)
     const int a = tid / D, bb = tid % D;
     int e = 0;
     for (int i = 0; i < K; i++) e |= (((a >> i) & 1) << h.lket[i]) | (((bb >> i) & 1) << h.lbra[i]);
-    const int run = e >> h.L;
+    const int run = e >> L;
     uint64_t off = 0;
-    for (int j = 0; j < h.mhi; j++) off |= (uint64_t)((run >> j) & 1) << h.hipos[j];
-    off += (uint64_t)(e & ((1 << h.L) - 1));
+    for (int j = 0; j < mhi; j++) off |= (uint64_t)((run >> j) & 1) << h.hipos[j];
+    off += (uint64_t)(e & ((1 << L) - 1));
     const uint64_t stored = (h.stmask[run >> 5] >> (run & 31)) & 1;
-    tb.outoff[a][bb] = off | ((uint64_t)(dp->ew[1][bb] + 128) << 48) | (stored << 63);
+    tb.outoff[bb][a] = off | ((uint64_t)(dp->ew[1][bb] + 128) << 48) | (stored << 63);
   }
+  if (tid < 8) tb.hipos[tid] = h.hipos[tid];
   if (tid < 256) tb.grp[tid >> 7].brmax[tid & 127] = 0;
   if (w == 0) {
     tc::tmem_alloc(&tb.slot, S::TMEM_COLS);
@@ -320,33 +342,45 @@ __global__ void __launch_bounds__(kT64Threads, 1)
   const uint32_t tmem = tb.slot + (uint32_t)g * S::SET_COLS;  // the group's accumulator set
   const uint32_t tlane = (uint32_t)(32 * (w & 3)) << 16;
 
-  int lf_g = 0;  // free-bit offset of this column's group f (the same in both steps)
-  for (int j = 0; j < h.g; j++) lf_g |= ((f >> j) & 1) << h.freepos[j];
-  const int L = h.L, runlen = 1 << L, ncopies = 2 << h.mhi;  // runs of the real and imaginary arrays
-  const uint64_t ntiles = h.ntiles, gstep = 2 * (uint64_t)gridDim.x;
-  // ket step: this thread's values (a, b = r, f), a = 0..D-1, of its half, at vals[posk[a]]
-  const uint64_t* vals = buf + (half ? TILE : 0);
+  auto free_off = [&](int ff) {  // local offset of free group ff
+    int o = 0;
+    for (int j = 0; j < h.g; j++) o |= ((ff >> j) & 1) << h.freepos[j];
+    return o;
+  };
+  const int lf = free_off(f);  // accumulator steps: free offset of column (., f) in the state
+  // digit steps: column (b = rc, fc)'s values a = 0..D-1 of half hc at buf[posk[a]]
   int posk[D];
   {
-    const int basek = tb.lb[r] + lf_g;
+    const int basec = hc * ASTR + tb.pb[rc] + piece_off(free_off(fc));
 #pragma unroll
-    for (int a = 0; a < D; a++) posk[a] = basek + tb.lk[a];
+    for (int a = 0; a < D; a++) posk[a] = basec + tb.pk[a];
   }
-  // The ket step's exact integer outputs replace the tile in its buffer, at
-  // [half][a][b ^ (a & 1)][f]: the ket step writes, for one a, 32 consecutive
-  // words per warp, and the bra step reads, for one b, columns a of both
-  // parities -- both free of bank conflicts.
-  auto yidx = [&](int a, int b) { return half * TILE + (a * D + (b ^ (a & 1))) * G + f; };
+  const uint64_t ntiles = h.ntiles, gstep = 2 * (uint64_t)gridDim.x;
+  const int runlen = 1 << L, lgp = L < 4 ? L : 4, npieces = (2 * TILE) >> lgp;
+  // The ket step's exact integer outputs Y(a, b) of column (b, ff) replace
+  // the tile in its buffer, at [hh][a][b ^ (a & 1)][ff]: the ket step writes,
+  // for one a, 32 consecutive words per warp, and the bra step reads, for one
+  // b, columns a of both parities -- both free of bank conflicts.
+  auto yoff = [&](int hh, int a, int b, int ff) { return hh * ASTR + (a * D + (b ^ (a & 1))) * G + ff; };
+  auto tile_base_s = [&](uint64_t t) {  // tile_base from the staged positions
+    uint64_t base = t << L;
+    for (int j = 0; j < mhi; j++) {
+      const int p = tb.hipos[j];
+      base = ((base >> p) << (p + 1)) | (base & ((1ull << p) - 1));
+    }
+    return base;
+  };
 
   // Loads of a tile into the group's buffer: the group's first thread arms
   // its barrier with the tile's bytes before a group barrier, after which
-  // every thread of the group issues its share of the 1-D bulk copies (one
-  // per run of each array).
-  auto copy_tile = [&](uint64_t t) {
-    const uint64_t base = tile_base(h, t);
-    for (int i = gtid; i < ncopies; i += kT64GroupThreads) {
-      const int run = i >> 1, arr = i & 1;
-      tc::bulk_g2s(buf + arr * TILE + run * runlen, (arr ? im : re) + base + tb.hioff[run], (uint32_t)runlen * 8u,
+  // every thread of the group issues its share of the 1-D bulk copies, one
+  // per piece (16 entries, or a whole run when runs are shorter) of each
+  // array.
+  auto copy_tile = [&](uint64_t base) {
+    for (int i = gtid; i < npieces; i += kT64GroupThreads) {
+      const int arr = i & 1, e0 = (i >> 1) << lgp;
+      const int run = e0 >> L, o = e0 & (runlen - 1);
+      tc::bulk_g2s(buf + arr * ASTR + piece_off(e0), (arr ? im : re) + base + tb.hioff[run] + o, 8u << lgp,
                    &gp.full);
     }
   };
@@ -368,59 +402,61 @@ __global__ void __launch_bounds__(kT64Threads, 1)
 
   // ---- prologue: the group's first tile in flight
   uint64_t t = blockIdx.x + (uint64_t)g * gridDim.x;
-  if (gtid == 0 && t < ntiles) tc::mbar_arrive_expect_tx(&gp.full, S::BUF_BYTES);
+  uint64_t tbase = t < ntiles ? tile_base_s(t) : 0;
+  if (gtid == 0 && t < ntiles) tc::mbar_arrive_expect_tx(&gp.full, S::TX_BYTES);
   group_bar(g);
   if (t < ntiles) {
-    copy_tile(t);
+    copy_tile(tbase);
     pendf = 1;
   }
 
   for (; t < ntiles; t += gstep) {
-    // ---- 1: the tile's values and their column maxima
+    // ---- 1: the tile's values of column (b = rc, fc), its grid (the largest
+    // exponent of both halves, one shuffle away), its ket digits
     wait(&gp.full, phf, pendf);
     {
+      uint64_t v[D];
       uint32_t emx = 0;
 #pragma unroll
-      for (int a = 0; a < D; a++) emx = max(emx, (uint32_t)(vals[posk[a]] >> 32) & 0x7FF00000u);
-      gp.colmax[half][m] = emx;
-    }
-    if (group_bar_or(g, bad)) break;
-
-    // ---- 2: ket digits of column (b = r, f) on its grid
-    uint32_t ecm = max(max(gp.colmax[0][m], gp.colmax[1][m]), 64u << 20);
-    const int Ec = (int)(ecm >> 20);
-    if (half == 0) gp.colEt[f][r] = Ec;
-#pragma unroll
-    for (int ch = 0; ch < D / 8; ch++) {
-      uint32_t pk[4][kTc64Slices];
-#pragma unroll
-      for (int c2 = 0; c2 < 4; c2++) {
-        float d0[kTc64Slices], d1[kTc64Slices];
-        const uint64_t v0 = vals[posk[8 * ch + 2 * c2]], v1 = vals[posk[8 * ch + 2 * c2 + 1]];
-        digits_fp64((uint32_t)v0, (uint32_t)(v0 >> 32), ecm, d0);
-        digits_fp64((uint32_t)v1, (uint32_t)(v1 >> 32), ecm, d1);
-#pragma unroll
-        for (int j = 0; j < kTc64Slices; j++) pk[c2][j] = pack_bf16x2(d0[j], d1[j]);
+      for (int a = 0; a < D; a++) {
+        v[a] = buf[posk[a]];
+        emx = max(emx, (uint32_t)(v[a] >> 32) & 0x7FF00000u);
       }
-      store_packed<8>(sA, S::A_BYTES, tc_kmajor_offset(m, half * D + 8 * ch, S::SBO), pk);
+      const uint32_t ecm = max(max(emx, __shfl_xor_sync(0xffffffffu, emx, 16)), 64u << 20);
+      if (hc == 0) gp.colEt[rc][fc] = (int)(ecm >> 20);
+#pragma unroll
+      for (int ch = 0; ch < D / 8; ch++) {
+        uint32_t pk[4][kTc64Slices];
+#pragma unroll
+        for (int c2 = 0; c2 < 4; c2++) {
+          float d0[kTc64Slices], d1[kTc64Slices];
+          const uint64_t v0 = v[8 * ch + 2 * c2], v1 = v[8 * ch + 2 * c2 + 1];
+          digits_fp64((uint32_t)v0, (uint32_t)(v0 >> 32), ecm, d0);
+          digits_fp64((uint32_t)v1, (uint32_t)(v1 >> 32), ecm, d1);
+#pragma unroll
+          for (int j = 0; j < kTc64Slices; j++) pk[c2][j] = pack_bf16x2(d0[j], d1[j]);
+        }
+        store_packed<8>(sA, S::A_BYTES, tc_kmajor_offset(mc, hc * D + 8 * ch, S::SBO), pk);
+      }
     }
     tc::fence_proxy_async_smem();
     tc::fence_before_sync();
-    group_bar(g);
+    if (group_bar_or(g, bad)) break;
     tc::fence_after_sync();
 
-    // ---- 3: ket products
+    // ---- 2: ket products
     if (gtid == 0) {
       issue_step<K>(sA, sB, tmem);
       tc::mma_commit(&gp.mma);
     }
     pendm = 1;
 
-    // ---- 4: ket outputs -> exact integers (in place of the tile), and the
-    // bra columns' magnitude keys: Ec + exponent of |S_0| + |S_1|/256 + 65,
-    // which bounds |Y| 2^Ec by 2^(key - 86) (1 + 2^-23)
+    // ---- 3: ket outputs of column (b = r, f) -> exact integers (in place of
+    // the tile), and the bra columns' magnitude keys: Ec + exponent of |S_0| +
+    // |S_1|/256 + 65, which bounds |Y| 2^Ec by 2^(key - 86) (1 + 2^-23)
     if (wait(&gp.mma, phm, pendm)) {
       tc::fence_after_sync();
+      const uint32_t Ec = (uint32_t)gp.colEt[r][f];
 #pragma unroll
       for (int c4 = 0; c4 < D; c4 += 4) {
         float sv[kTc64Orders][4];
@@ -431,10 +467,10 @@ __global__ void __launch_bounds__(kT64Threads, 1)
 #pragma unroll
         for (int c = 0; c < 4; c++) {
           const int a = c4 + c;
-          buf[yidx(a, r)] = (uint64_t)combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c],
-                                                     sv[6][c], sv[7][c]);
+          buf[yoff(half, a, r, f)] = (uint64_t)combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c],
+                                                              sv[5][c], sv[6][c], sv[7][c]);
           const float mag = fmaf(fabsf(sv[1][c]), 0.00390625f, fabsf(sv[0][c])) + 65.0f;
-          atomicMax(&gp.brmax[a * G + f], (uint32_t)Ec + (__float_as_uint(mag) >> 23));
+          atomicMax(&gp.brmax[a * G + f], Ec + (__float_as_uint(mag) >> 23));
         }
       }
     }
@@ -442,52 +478,56 @@ __global__ void __launch_bounds__(kT64Threads, 1)
     if (group_bar_or(g, bad)) break;
     tc::fence_after_sync();
 
-    // ---- 5: bra digits of column (a = r, f): values Y_b 2^Ec(b) on the grid
-    // 2^(mkey - 141), |v| < 2^55 (1 + 2^-23)
-    const uint32_t mkey = gp.brmax[m];
+    // ---- 4: bra digits of column (a = rc, fc): values Y_b 2^Ec(b) on the
+    // grid 2^(mkey - 141), |v| < 2^55 (1 + 2^-23)
+    const uint32_t mkey_out = gp.brmax[m];  // the key of this thread's column in step 6
+    {
+      const uint32_t mkey = gp.brmax[mc];
 #pragma unroll
-    for (int ch = 0; ch < D / 8; ch++) {
-      uint32_t pk[4][kTc64Slices];
+      for (int ch = 0; ch < D / 8; ch++) {
+        uint32_t pk[4][kTc64Slices];
 #pragma unroll
-      for (int c2 = 0; c2 < 4; c2++) {
-        float d[2][kTc64Slices];
+        for (int c2 = 0; c2 < 4; c2++) {
+          float d[2][kTc64Slices];
 #pragma unroll
-        for (int u = 0; u < 2; u++) {
-          const int b = 8 * ch + 2 * c2 + u;
-          const int64_t Y = (int64_t)buf[yidx(r, b)];
-          const int sh = (int)mkey - 141 - gp.colEt[f][b];
-          const int64_t v = sh >= 0 ? shr_s64(Y, (uint32_t)sh) : shl_s64(Y, (uint32_t)(-sh));
-          digits_int(v, d[u]);
+          for (int u = 0; u < 2; u++) {
+            const int b = 8 * ch + 2 * c2 + u;
+            const int64_t Y = (int64_t)buf[yoff(hc, rc, b, fc)];
+            const int sh = (int)mkey - 141 - gp.colEt[b][fc];
+            const int64_t v = sh >= 0 ? shr_s64(Y, (uint32_t)sh) : shl_s64(Y, (uint32_t)(-sh));
+            digits_int(v, d[u]);
+          }
+#pragma unroll
+          for (int j = 0; j < kTc64Slices; j++) pk[c2][j] = pack_bf16x2(d[0][j], d[1][j]);
         }
-#pragma unroll
-        for (int j = 0; j < kTc64Slices; j++) pk[c2][j] = pack_bf16x2(d[0][j], d[1][j]);
+        store_packed<8>(sA, S::A_BYTES, tc_kmajor_offset(mc, hc * D + 8 * ch, S::SBO), pk);
       }
-      store_packed<8>(sA, S::A_BYTES, tc_kmajor_offset(m, half * D + 8 * ch, S::SBO), pk);
     }
     const uint64_t tn = t + gstep;
-    if (gtid == 0 && tn < ntiles) tc::mbar_arrive_expect_tx(&gp.full, S::BUF_BYTES);  // the group's next tile
+    if (gtid == 0 && tn < ntiles) tc::mbar_arrive_expect_tx(&gp.full, S::TX_BYTES);  // the group's next tile
     tc::fence_proxy_async_smem();
     tc::fence_before_sync();
     group_bar(g);
     tc::fence_after_sync();
 
-    // ---- 6: bra products; the group's next tile into the freed buffer
+    // ---- 5: bra products; the group's next tile into the freed buffer
     if (gtid == 0) {
       issue_step<K>(sA, sB + kTc64Slices * S::B_BYTES, tmem);
       tc::mma_commit(&gp.mma);
     }
     pendm = 1;
     if (gtid < 128) gp.brmax[gtid] = 0;  // the next tile's magnitude keys
+    const uint64_t nbase = tn < ntiles ? tile_base_s(tn) : 0;
     if (tn < ntiles) {
-      copy_tile(tn);
+      copy_tile(nbase);
       pendf = 1;
     }
 
-    // ---- 7: bra outputs -> FP64 -> the tile's stored runs
+    // ---- 6: bra outputs of column (a = r, f) -> FP64 -> the tile's stored runs
     if (wait(&gp.mma, phm, pendm)) {
       tc::fence_after_sync();
-      const int pa = (int)mkey + tb.ew[0][r] - 1106 - 128;
-      uint64_t* arr = (half ? im : re) + tile_base(h, t) + lf_g;
+      const int pa = (int)mkey_out + tb.ew[0][r] - 1106 - 128;
+      uint64_t* arr = (half ? im : re) + tbase + lf;
 #pragma unroll
       for (int c4 = 0; c4 < D; c4 += 4) {
         float sv[kTc64Orders][4];
@@ -497,7 +537,7 @@ __global__ void __launch_bounds__(kT64Threads, 1)
         tc::tmem_wait_ld();
 #pragma unroll
         for (int c = 0; c < 4; c++) {
-          const uint64_t T = tb.outoff[r][c4 + c];
+          const uint64_t T = tb.outoff[c4 + c][r];
           if (!(T >> 63)) continue;  // a run the pass does not change
           const int64_t Y =
               combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c], sv[6][c], sv[7][c]);
@@ -505,7 +545,8 @@ __global__ void __launch_bounds__(kT64Threads, 1)
         }
       }
     }
-    tc::fence_before_sync();  // the next tile's first barrier orders these reads before its MMAs
+    tc::fence_before_sync();  // the next tile's first group barrier orders these reads before its MMAs
+    tbase = nbase;
   }
 
   // ---- teardown: nothing of this group may still be in flight when the
@@ -525,6 +566,7 @@ __global__ void __launch_bounds__(kT64Threads, 1)
 template <int K>
 static cudaError_t configure_tc64() {
   constexpr size_t smem = t64_smem_bytes<K>();
+  static_assert(smem <= 227 * 1024, "one block's shared memory");
   cudaError_t e = cudaFuncSetAttribute(k_pass_tc64<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_pass_tc64<K>, cudaFuncAttributePreferredSharedMemoryCarveout,
