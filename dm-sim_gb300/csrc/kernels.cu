@@ -16,6 +16,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "kernels.h"
 #include "pass.h"
@@ -23,6 +24,17 @@
 #include "pass_kernel.cuh"
 
 namespace dmg {
+
+// 3- and 4-qubit SPARSE passes of complex64 states run as dense ones: on the
+// FP32 pipe a dense row is 4 * 2^K multiply-adds fed by 16-byte broadcast
+// coefficient loads, where the sparse row walk costs several dependent
+// shared-memory loads per nonzero and runs slower at every density these
+// fused blocks have.  (FP64 and double-float keep the sparse walk: their
+// multiply-adds, not the loads, bound them.)
+template <typename T, int K>
+constexpr bool sparse_as_dense() {
+  return std::is_same<T, float>::value && K >= 3;
+}
 
 template <typename T, int K>
 static cudaError_t launch_k(const LaunchArgs& a, cudaStream_t s) {
@@ -35,6 +47,7 @@ static cudaError_t launch_k(const LaunchArgs& a, cudaStream_t s) {
       return launch_one<T, K, CLS_DENSE>(a, s);
     case CLS_SPARSE:
       if (a.real && K <= 2) return launch_pass_real(a, s);
+      if (sparse_as_dense<T, K>()) return launch_one<T, K, CLS_DENSE>(a, s);
       return launch_one<T, K, CLS_SPARSE>(a, s);
     case CLS_RLIN:
       if (K == 1) return launch_one<T, 1, CLS_RLIN>(a, s);
@@ -82,7 +95,7 @@ static int occ_k(int cls) {
     case CLS_SIGNED: return occ_one<T, K, CLS_SIGNED>();
     case CLS_PHASE: return occ_one<T, K, CLS_PHASE>();
     case CLS_DENSE: return occ_one<T, K, CLS_DENSE>();
-    case CLS_SPARSE: return occ_one<T, K, CLS_SPARSE>();
+    case CLS_SPARSE: return sparse_as_dense<T, K>() ? occ_one<T, K, CLS_DENSE>() : occ_one<T, K, CLS_SPARSE>();
     case CLS_SUPER: return K <= 1 ? occ_one<T, 1, CLS_SUPER>() : occ_one<T, 2, CLS_SUPER>();
     default: return occ_one<T, 1, CLS_RLIN>();
   }

@@ -211,6 +211,21 @@ __device__ __forceinline__ typename Vec2<T>::type ld_pair(const T* s, int e) {
   return v;
 }
 
+// V consecutive coefficients of a dense row as one 16-byte shared-memory
+// vector load: every thread of the block reads the same address (a
+// broadcast), so a row of 2^K complex terms costs 2^K / V loads of each of
+// U's real and imaginary parts instead of 2^K.  Rows of 3- and 4-qubit
+// operators only (the narrow rows keep scalar loads and their register
+// budget).
+template <typename T, int D>
+struct CoefVec {
+  static constexpr int V = D < 8 ? 1 : 16 / (int)sizeof(T);
+  struct alignas(V * sizeof(T)) Pack {
+    T v[V];
+  };
+  __device__ __forceinline__ static Pack load(const T* p) { return *reinterpret_cast<const Pack*>(p); }
+};
+
 // Per-pass constant tables, staged in shared memory once per block (or once
 // per work-queue range).  Arrays a class does not use shrink to one element.
 template <typename T, int K, int CLS_>
@@ -222,7 +237,11 @@ struct PassTables {
   uint32_t ldmask[8], stmask[8];
   int lk[D], lb[D];  // swizzled shared-memory offsets (tile_sw) of the ket / bra indices
   int lket[4], lbra[4];
-  T ure[kMat ? D * D : 1], uim[kMat ? D * D : 1], vre[kMat ? D * D : 1], vim[kMat ? D * D : 1];
+  // 16-byte aligned: the dense rows read them as 16-byte broadcast vectors
+  alignas(16) T ure[kMat ? D * D : 1];
+  alignas(16) T uim[kMat ? D * D : 1];
+  alignas(16) T vre[kMat ? D * D : 1];
+  alignas(16) T vim[kMat ? D * D : 1];
   T fre[CLS == CLS_PHASE ? D * D : 1], fim[CLS == CLS_PHASE ? D * D : 1];
   T rl[32];
   int8_t fk[D * D];
@@ -475,15 +494,32 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
 #pragma unroll
         for (int a = 0; a < D; a++) {
           Acc<T> ar, ai;
+          using CV = CoefVec<T, D>;
 #pragma unroll
-          for (int c = 0; c < D; c++) {
-            const T ur = tb.ure[a * D + c];
-            ar.mad(ur, xr[c]);
-            ai.mad(ur, xi[c]);
-            if constexpr (!RE) {
-              const T ui = tb.uim[a * D + c];
-              ar.mad(-ui, xi[c]);
-              ai.mad(ui, xr[c]);
+          for (int c0 = 0; c0 < D; c0 += CV::V) {
+            if constexpr (CV::V == 1) {
+              const T ur = tb.ure[a * D + c0];
+              ar.mad(ur, xr[c0]);
+              ai.mad(ur, xi[c0]);
+              if constexpr (!RE) {
+                const T ui = tb.uim[a * D + c0];
+                ar.mad(-ui, xi[c0]);
+                ai.mad(ui, xr[c0]);
+              }
+            } else {
+              const typename CV::Pack ur = CV::load(&tb.ure[a * D + c0]);
+              typename CV::Pack ui;
+              if constexpr (!RE) ui = CV::load(&tb.uim[a * D + c0]);
+#pragma unroll
+              for (int v = 0; v < CV::V; v++) {
+                const int c = c0 + v;
+                ar.mad(ur.v[v], xr[c]);
+                ai.mad(ur.v[v], xi[c]);
+                if constexpr (!RE) {
+                  ar.mad(-ui.v[v], xi[c]);
+                  ai.mad(ui.v[v], xr[c]);
+                }
+              }
             }
           }
           sre[cb ^ tb.lk[a]] = ar.get();
@@ -539,15 +575,32 @@ __device__ void tile_body(T* __restrict__ re, T* __restrict__ im, const PassHead
 #pragma unroll
         for (int b = 0; b < D; b++) {
           Acc<T> ar, ai;
+          using CV = CoefVec<T, D>;
 #pragma unroll
-          for (int c = 0; c < D; c++) {
-            const T vr = tb.vre[b * D + c];
-            ar.mad(vr, xr[c]);
-            ai.mad(vr, xi[c]);
-            if constexpr (!RE) {
-              const T vi = tb.vim[b * D + c];
-              ar.mad(-vi, xi[c]);
-              ai.mad(vi, xr[c]);
+          for (int c0 = 0; c0 < D; c0 += CV::V) {
+            if constexpr (CV::V == 1) {
+              const T vr = tb.vre[b * D + c0];
+              ar.mad(vr, xr[c0]);
+              ai.mad(vr, xi[c0]);
+              if constexpr (!RE) {
+                const T vi = tb.vim[b * D + c0];
+                ar.mad(-vi, xi[c0]);
+                ai.mad(vi, xr[c0]);
+              }
+            } else {
+              const typename CV::Pack vr = CV::load(&tb.vre[b * D + c0]);
+              typename CV::Pack vi;
+              if constexpr (!RE) vi = CV::load(&tb.vim[b * D + c0]);
+#pragma unroll
+              for (int v = 0; v < CV::V; v++) {
+                const int c = c0 + v;
+                ar.mad(vr.v[v], xr[c]);
+                ai.mad(vr.v[v], xi[c]);
+                if constexpr (!RE) {
+                  ar.mad(-vi.v[v], xi[c]);
+                  ai.mad(vi.v[v], xr[c]);
+                }
+              }
             }
           }
           sre[ca ^ tb.lb[b]] = ar.get();

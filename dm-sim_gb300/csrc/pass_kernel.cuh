@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "kernels.h"
 #include "pass.h"
 #include "pass_device.cuh"
@@ -27,7 +29,7 @@ __global__ void __launch_bounds__(kThreads) k_pass(T* __restrict__ re, T* __rest
   // Full-size tiles of narrow passes (2^(K-1) entry pairs per thread): the
   // next tile's loads go out before the current tile is transformed.
   constexpr int P = K >= 1 ? 1 << (K - 1) : 1;
-  if constexpr (K >= 1 && K <= 2) {
+  if constexpr ((K >= 1 && K <= 2) || (std::is_same<T, float>::value && base_class(CLS) == CLS_DENSE)) {
     if (tile == 2 * kThreads * P) {
       uint64_t t = blockIdx.x;
       if (t >= h.ntiles) return;
