@@ -17,7 +17,7 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libdmsim_gb300.so")
 INCLUDE = os.path.normpath(os.path.join(HERE, "..", "include"))
 
-SOURCES = ["kernels.cu", "kernels_real.cu", "kernels_k1.cu", "tensor.cu", "tensor64.cu", "metrics.cu", "mlp.cu", "batch.cu", "peaks.cu", "engine.cpp", "gates.cpp", "plan.cpp", "costmodel.cpp",
+SOURCES = ["kernels.cu", "kernels_real.cu", "kernels_k1.cu", "tensor.cu", "tensor64.cu", "tensor32.cu", "metrics.cu", "mlp.cu", "batch.cu", "peaks.cu", "engine.cpp", "gates.cpp", "plan.cpp", "costmodel.cpp",
            "batch.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE]

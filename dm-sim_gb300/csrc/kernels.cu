@@ -72,7 +72,11 @@ static cudaError_t launch_t(const LaunchArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_pass(const LaunchArgs& a, cudaStream_t s) {
-  if (a.tc) return a.arith == AR_FP64 ? launch_pass_tc64(a, s) : launch_pass_tc(a, s);
+  if (a.tc) {
+    if (a.arith == AR_FP64) return launch_pass_tc64(a, s);
+    if (a.arith == AR_FP32) return launch_pass_tc32(a, s);
+    return launch_pass_tc(a, s);
+  }
   if (a.direct1) return launch_pass1(a, s);
   if (a.arith == AR_DF64) return launch_t<df64>(a, s);
   return a.fp32 ? launch_t<float>(a, s) : launch_t<double>(a, s);

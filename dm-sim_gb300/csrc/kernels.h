@@ -37,6 +37,9 @@ cudaError_t launch_pass_real(const LaunchArgs& a, cudaStream_t s);
 // Tensor-core passes (tensor.cu): launch, and resident blocks per SM.
 cudaError_t launch_pass_tc(const LaunchArgs& a, cudaStream_t s);
 int tc_blocks_per_sm(int K, int arith);
+// Tensor-core passes on a complex64 (FP32) state (tensor32.cu): two
+// persistent 512-thread blocks per SM.
+cudaError_t launch_pass_tc32(const LaunchArgs& a, cudaStream_t s);
 // FP64-width tensor-core passes on an FP64 state (tensor64.cu): one
 // persistent 512-thread block per SM.
 cudaError_t launch_pass_tc64(const LaunchArgs& a, cudaStream_t s);

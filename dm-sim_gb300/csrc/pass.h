@@ -139,7 +139,8 @@ struct TcDesc {
   PassHeader h;  // tile geometry, g = 7 - K (128 columns per step)
   // slices of W (0) and V (1): row n of W = sum_j sl[0][j][n][.], slice j on
   // the grid 2^(e_n - 7 - 8j) with |W[n][.]| < 2^e_n (BF16 bits at true
-  // scale, K-major core-matrix layout)
+  // scale, K-major core-matrix layout).  For a complex64 state, slices 0..2
+  // hold each entry's own BF16 x 3 split (hi, mid, lo) instead.
   alignas(16) uint16_t sl[2][kTcSlices][R * R];
 };
 

@@ -180,6 +180,40 @@ std::vector<PassSpec> plan_greedy(const std::vector<Basic>& basics, int maxk, in
   const int kWindow = 96;  // look-ahead over untaken gates
   int first = 0;
   std::vector<int> cand;
+  std::vector<char> blocked(nqb, 0);
+  // Gates of the window (from the first untaken gate) that a pass holding
+  // ps's qubits plus those of gate j could take, j included: a gate is
+  // absorbable when all its qubits are in the set and none of them is held
+  // by an earlier untaken gate that is not.
+  auto absorb_count = [&](int j, const PassSpec& ps) {
+    int qs[kMaxK + 2], nqs = 0;
+    for (int i = 0; i < ps.K; i++) qs[nqs++] = ps.q[i];
+    for (int t = 0; t < nq(basics[j]); t++) {
+      bool in = false;
+      for (int i = 0; i < nqs; i++) in |= qs[i] == basics[j].q[t];
+      if (!in) qs[nqs++] = basics[j].q[t];
+    }
+    auto member = [&](int q) {
+      for (int i = 0; i < nqs; i++)
+        if (qs[i] == q) return true;
+      return false;
+    };
+    std::fill(blocked.begin(), blocked.end(), 0);
+    int count = 0, seen = 0;
+    for (int k = first; k < m && seen < kWindow; k++) {
+      if (taken[k]) continue;
+      seen++;
+      const Basic& b = basics[k];
+      bool ok = b.kind != BK_RLIN && b.kind != BK_SUPER;
+      for (int t = 0; t < nq(b); t++) ok = ok && member(b.q[t]) && !blocked[b.q[t]];
+      if (ok) {
+        count++;
+      } else {
+        for (int t = 0; t < nq(b); t++) blocked[b.q[t]] = 1;
+      }
+    }
+    return count;
+  };
   while (first < m) {
     while (first < m && taken[first]) first++;
     if (first >= m) break;
@@ -223,6 +257,18 @@ std::vector<PassSpec> plan_greedy(const std::vector<Basic>& basics, int maxk, in
       }
       if (cand.empty()) break;
       std::sort(cand.begin(), cand.end());
+      // When every candidate widens the pass, the qubit it brings decides
+      // which later gates the pass can still take: rank those candidates by
+      // how many gates of the window the widened qubit set would absorb
+      // (program order on every qubit respected), most first, then by the
+      // order above.
+      if (cand.front() / m > 0 && p.K < maxk) {
+        std::vector<std::pair<int, int>> ranked;  // (-absorbed, key)
+        ranked.reserve(cand.size());
+        for (int key : cand) ranked.push_back({-absorb_count(key % m, p), key});
+        std::stable_sort(ranked.begin(), ranked.end());
+        for (size_t i = 0; i < cand.size(); i++) cand[i] = ranked[i].second;
+      }
       bool grown = false;
       for (int key : cand) {
         const int j = key % m;
@@ -527,9 +573,21 @@ uint64_t build_k(const PassSpec& p, int n, PassDesc<K>* d, PassFeatures* feat, u
 // Tensor-core pass: the geometry of the K-qubit pass with 2^(7-K) groups per
 // tile (128 columns per step), every run loaded, and the BF16 slices of the
 // real embeddings of U (ket) and V (bra).
+// x rounded to the nearest BF16 value (8 significant bits, ties to even), as
+// a float.
+float bf16_round(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  if ((u & 0x7F800000u) == 0x7F800000u) return x;  // inf / nan: unchanged
+  u = (u + 0x7FFFu + ((u >> 16) & 1u)) & 0xFFFF0000u;
+  float r;
+  std::memcpy(&r, &u, 4);
+  return r;
+}
+
 template <int K>
 uint64_t build_tc_k(const PassSpec& p, int n, TcDesc<K>* d, PassFeatures* feat, uint64_t* ntiles_out,
-                    int* tile_out, bool slices) {
+                    int* tile_out, bool slices, bool per_entry) {
   constexpr int D = 1 << K, R = 2 * D;
   std::unique_ptr<PassDesc<K>> geo(new PassDesc<K>);
   build_k<K>(p, n, geo.get(), feat, ntiles_out, tile_out, 7 - K);
@@ -552,6 +610,24 @@ uint64_t build_tc_k(const PassSpec& p, int n, TcDesc<K>* d, PassFeatures* feat, 
         const cplx m = M[a * D + (k % D)];
         if (row < D) w[k] = k < D ? m.real() : -m.imag();
         else w[k] = k < D ? m.imag() : m.real();
+      }
+      if (per_entry) {
+        // complex64 state: each entry of the FP32-rounded operator as the sum
+        // of three BF16 values (hi, mid, lo), each rounded from the remainder
+        // of the ones before it
+        for (int k = 0; k < R; k++) {
+          float v = (float)w[k];
+          for (int j = 0; j < kTcSlices; j++) {
+            uint32_t bits = 0;
+            if (j < 3) {
+              const float t = bf16_round(v);
+              std::memcpy(&bits, &t, 4);
+              v -= t;  // exact: the remainder of a rounding to 8 significant bits
+            }
+            d->sl[side][j][tc_kmajor_offset(row, k, 16 * R) / 2] = (uint16_t)(bits >> 16);
+          }
+        }
+        continue;
       }
       double mx = 0;
       for (int k = 0; k < R; k++) mx = std::max(mx, std::fabs(w[k]));
@@ -637,8 +713,11 @@ uint64_t build_tc_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uin
     if (p.K == 3) return build_tc64_k<3>(p, n, static_cast<TcDesc64<3>*>(out), f, ntiles, tile_entries, slices);
     return build_tc64_k<4>(p, n, static_cast<TcDesc64<4>*>(out), f, ntiles, tile_entries, slices);
   }
-  if (p.K == 3) return build_tc_k<3>(p, n, static_cast<TcDesc<3>*>(out), f, ntiles, tile_entries, slices);
-  return build_tc_k<4>(p, n, static_cast<TcDesc<4>*>(out), f, ntiles, tile_entries, slices);
+  // complex64 (arith 1): per-entry BF16 x 3 slices (tensor32.cu); double-float:
+  // 6 slices on per-row grids (tensor.cu)
+  const bool per_entry = arith == 1;
+  if (p.K == 3) return build_tc_k<3>(p, n, static_cast<TcDesc<3>*>(out), f, ntiles, tile_entries, slices, per_entry);
+  return build_tc_k<4>(p, n, static_cast<TcDesc<4>*>(out), f, ntiles, tile_entries, slices, per_entry);
 }
 
 bool tc_eligible(const PassSpec& p, int n) {
@@ -652,9 +731,12 @@ bool tc_eligible(const PassSpec& p, int n) {
 bool tc_choose(const PassSpec& p, int n, int tensor_opt, int arith) {
   if (!tensor_opt || !tc_eligible(p, n)) return false;
   if (tensor_opt == 2) return true;  // every eligible pass (measurements)
-  if (arith == 1) return false;      // complex64: opt-in only (option 2)
   if (p.tc >= 0) return p.tc != 0;   // the learned planner's choice
   if (arith == 0) return true;       // FP64: the alternative is GB300's FP64 pipe
+  // complex64: 4-qubit passes on the tensor cores (tensor32.cu: 2530 against
+  // 1790 GB/s for the FP32-pipe kernel at 14 qubits); 3-qubit ones stay on the
+  // FP32 pipe (2820 against 2360 GB/s)
+  if (arith == 1) return p.K == 4;
   return p.nnz >= kTcMinRowNnz * (1 << p.K);
 }
 

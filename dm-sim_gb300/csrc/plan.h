@@ -81,6 +81,8 @@ size_t tc_desc_bytes(int K, int arith = 2);
 // slices = false: geometry and features only (the planner's scoring).
 uint64_t build_tc_desc(const PassSpec& p, int n, void* out, PassFeatures* f, uint64_t* ntiles, int* tile_entries,
                        bool slices = true, int arith = 2);
+// x rounded to the nearest BF16 value, as a float.
+float bf16_round(float x);
 // The 7 balanced base-256 digits of an integer |t| <= 2^55 (digit 0 the most
 // significant, weight 256^(6-j)): t = sum_j d[j] 256^(6-j), |d[j]| <= 128.
 void tc64_digits(int64_t t, int d[7]);

@@ -500,7 +500,7 @@ static int tc_occ() {
 
 int tc_blocks_per_sm(int K, int arith) {
   if (arith == AR_FP64) return 1;  // the FP64-width kernel: one persistent block per SM (tensor64.cu)
-  if (arith == AR_FP32) return K == 3 ? tc_occ<3, float>() : tc_occ<4, float>();
+  if (arith == AR_FP32) return 2;  // the complex64 kernel: two persistent blocks per SM (tensor32.cu)
   return K == 3 ? tc_occ<3, df64>() : tc_occ<4, df64>();
 }
 

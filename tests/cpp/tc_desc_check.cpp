@@ -110,6 +110,39 @@ static bool check(const PassSpec& p, int n) {
   return true;
 }
 
+// complex64 descriptors: every operator entry as the sum of three BF16
+// values (h, m, l), within 2^-24 of the entry rounded to FP32; slices 3..
+// empty.
+template <int K>
+static bool check_c64(const PassSpec& p, int n) {
+  constexpr int D = 1 << K, R = 2 * D;
+  std::unique_ptr<TcDesc<K>> d(new TcDesc<K>);
+  uint64_t ntiles = 0;
+  int tile = 0;
+  build_tc_desc(p, n, d.get(), nullptr, &ntiles, &tile, true, 1);
+  for (int side = 0; side < 2; side++) {
+    const cplx* M = side ? p.V : p.U;
+    for (int row = 0; row < R; row++)
+      for (int k = 0; k < R; k++) {
+        const cplx v = M[(row % D) * D + (k % D)];
+        const double w = row < D ? (k < D ? v.real() : -v.imag()) : (k < D ? v.imag() : v.real());
+        const float wf = (float)w;
+        const uint32_t off = tc_kmajor_offset(row, k, 16 * R) / 2;
+        double sum = 0, prev = 1e300;
+        for (int j = 0; j < kTcSlices; j++) {
+          const double t = bf16_to_float(d->sl[side][j][off]);
+          if (j >= 3 && t != 0) return std::printf("c64 slice %d not empty\n", j), false;
+          if (j < 3 && t != 0 && std::fabs(t) > prev) return std::printf("c64 slices not decreasing\n"), false;
+          if (t != 0) prev = std::fabs(t);
+          sum += t;
+        }
+        if (std::fabs(sum - (double)wf) > std::ldexp(std::fabs((double)wf), -24))
+          return std::printf("c64 row %d col %d: %.9g vs %.9g\n", row, k, sum, (double)wf), false;
+      }
+  }
+  return true;
+}
+
 int main() {
   std::mt19937_64 rng(7);
   int checked = 0;
@@ -136,7 +169,7 @@ int main() {
     for (int k : {3, 4}) {
       for (const PassSpec& p : plan_greedy(basics, k, 16)) {
         if (!tc_eligible(p, n)) continue;
-        const bool ok = p.K == 3 ? check<3>(p, n) : check<4>(p, n);
+        const bool ok = p.K == 3 ? (check<3>(p, n) && check_c64<3>(p, n)) : (check<4>(p, n) && check_c64<4>(p, n));
         if (!ok) return std::printf("failed: n=%d K=%d\n", n, p.K), 1;
         checked++;
       }

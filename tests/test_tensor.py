@@ -116,3 +116,49 @@ def test_complex64_tensor_passes(engine):
     assert errs["all"][1] and not errs[0][1]
     assert errs["all"][0] <= 1e-5 and errs[0][0] <= 1e-5, errs
     assert errs["all"][0] <= 4 * errs[0][0] + 1e-7, errs
+
+
+@pytest.mark.parametrize("max_k", [3, 4])
+def test_complex64_tensor_kernel_12q(engine, max_k):
+    """The complex64 tensor-core kernel (tensor32.cu: 3 true-scale BF16 slices,
+    exact FP32 order sums) at 12 qubits, every 3- or 4-qubit pass on it:
+    against an FP64 run of the same circuit, at the FP32-pipe passes' error
+    level (complex64: tolerance 1e-5 max element)."""
+    n = 12
+    circ = W.u3_cx_ccx(n, 400, seed=21)
+    errs = {}
+    with engine.Simulation(n, mode="fused", max_k=max_k) as ref:
+        ref.extend(circ)
+        ref.upload()
+        ref.run()
+        for tensor in (0, "all"):
+            with engine.Simulation(n, mode="fused", max_k=max_k, precision="c64", tensor=tensor) as s:
+                s.extend(circ)
+                s.upload()
+                s.set_option(engine.OPT_RECORD, 1)
+                s.run()
+                rec = s.pass_records()
+                ntc = int(rec[:, 8].sum())
+                widths = set(int(k) for k in rec[rec[:, 8] > 0, 0])
+                errs[tensor] = (s.compare(ref)["max_abs_err"], ntc, widths)
+    assert errs[0][1] == 0 and errs["all"][1] > 0, errs
+    assert max_k in errs["all"][2], errs
+    assert errs["all"][0] <= 1e-5 and errs[0][0] <= 1e-5, errs
+    assert errs["all"][0] <= 4 * errs[0][0] + 1e-7, errs
+
+
+@pytest.mark.parametrize("n,seed", [(6, 5), (8, 6)])
+def test_complex64_tensor_kernel_vs_oracle(engine, oracle, n, seed):
+    """complex64 state, every eligible pass on the complex64 tensor kernel,
+    against the CPU oracle (FP64) on the mixed-gate table: within complex64
+    accuracy."""
+    circ = W.table_mix(n, 150, seed=seed)
+    with engine.Simulation(n, mode="fused", precision="c64", tensor="all") as s:
+        s.extend(circ)
+        s.upload()
+        s.set_option(engine.OPT_RECORD, 1)
+        s.run()
+        assert s.pass_records()[:, 8].sum() > 0
+        re, im = s.get_dm()
+    ref = oracle.dm_sim(n, circ)
+    assert maxerr((re, im), ref) <= 2e-5 * max(1.0, np.abs(ref[0]).max())
