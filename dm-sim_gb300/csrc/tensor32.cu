@@ -82,6 +82,10 @@ struct T32Tables {
   // output (a, b) of a tile, at [b][a]: bits 0..47 its offset from the tile
   // base minus the free bits, bit 63 set when its run is stored
   uint64_t outoff[D][D];
+  // the same offsets split by their disjoint bit fields: output (a, b) at
+  // offk[a] + offb[b]; allstored: every run of the tile is stored
+  uint64_t offk[D], offb[D];
+  int allstored;
   T32Group grp[2];
   int pk[D], pb[D];  // piece_off32 of the ket / bra index bits
   int hipos[8];
@@ -142,6 +146,13 @@ __device__ __forceinline__ void slice_column(const float (&v)[D], int row, int h
     for (int j = 0; j < kT32Slices; j++)
       *reinterpret_cast<uint4*>(sA + j * A_BYTES + off) = make_uint4(pk[0][j], pk[1][j], pk[2][j], pk[3][j]);
   }
+}
+
+// This warp's D consecutive TMEM columns (32 lanes) in one load.
+template <int D>
+__device__ __forceinline__ void tmem_ld_row(uint32_t taddr, float (&v)[D]) {
+  if constexpr (D == 16) tc::tmem_ld16(taddr, v);
+  else tc::tmem_ld8(taddr, v);
 }
 
 // One thread issues every product of a step: slice pairs (i of the columns,
@@ -224,6 +235,21 @@ __global__ void __launch_bounds__(kT32Threads, 2)
     off += (uint64_t)(e & ((1 << L) - 1));
     const uint64_t stored = (h.stmask[run >> 5] >> (run & 31)) & 1;
     tb.outoff[bb][a] = off | (stored << 63);
+  }
+  if (tid < 2 * D) {
+    const int i = tid & (D - 1), side = tid / D;  // side 0: ket index i, 1: bra index i
+    int e = 0;
+    for (int k = 0; k < K; k++) e |= ((i >> k) & 1) << (side ? h.lbra[k] : h.lket[k]);
+    const int run = e >> L;
+    uint64_t off = 0;
+    for (int j = 0; j < mhi; j++) off |= (uint64_t)((run >> j) & 1) << h.hipos[j];
+    off += (uint64_t)(e & ((1 << L) - 1));
+    (side ? tb.offb : tb.offk)[i] = off;
+  }
+  if (tid == 0) {
+    int all = 1;
+    for (int run = 0; run < (1 << mhi); run++) all &= (int)((h.stmask[run >> 5] >> (run & 31)) & 1);
+    tb.allstored = all;
   }
   if (tid < 8) tb.hipos[tid] = h.hipos[tid];
   if (w == 0) {
@@ -333,14 +359,11 @@ __global__ void __launch_bounds__(kT32Threads, 2)
     // ---- 3: ket outputs of column (b = r, f), in place of the tile
     if (wait(&gp.mma, phm, pendm)) {
       tc::fence_after_sync();
+      float sv[D];
+      tmem_ld_row<D>(tmem + tlane + half * D, sv);
+      tc::tmem_wait_ld();
 #pragma unroll
-      for (int c8 = 0; c8 < D; c8 += 8) {
-        float sv[8];
-        tc::tmem_ld8(tmem + tlane + half * D + c8, sv);
-        tc::tmem_wait_ld();
-#pragma unroll
-        for (int c = 0; c < 8; c++) buf[yoff(half, c8 + c, r, f)] = sv[c];
-      }
+      for (int a = 0; a < D; a++) buf[yoff(half, a, r, f)] = sv[a];
     }
     tc::fence_before_sync();
     if (group_bar_or32(g, bad)) break;
@@ -376,16 +399,19 @@ __global__ void __launch_bounds__(kT32Threads, 2)
     if (wait(&gp.mma, phm, pendm)) {
       tc::fence_after_sync();
       float* arr = (half ? im : re) + tbase + lf;
+      float sv[D];
+      tmem_ld_row<D>(tmem + tlane + half * D, sv);
+      tc::tmem_wait_ld();
+      if (tb.allstored) {  // the common case: one base per thread, one offset per output
+        float* col = arr + tb.offk[r];
 #pragma unroll
-      for (int c8 = 0; c8 < D; c8 += 8) {
-        float sv[8];
-        tc::tmem_ld8(tmem + tlane + half * D + c8, sv);
-        tc::tmem_wait_ld();
+        for (int b = 0; b < D; b++) col[tb.offb[b]] = sv[b];
+      } else {
 #pragma unroll
-        for (int c = 0; c < 8; c++) {
-          const uint64_t T = tb.outoff[c8 + c][r];
+        for (int b = 0; b < D; b++) {
+          const uint64_t T = tb.outoff[b][r];
           if (!(T >> 63)) continue;  // a run the pass does not change
-          arr[T & 0xFFFFFFFFFFFFull] = sv[c];
+          arr[T & 0xFFFFFFFFFFFFull] = sv[b];
         }
       }
     }

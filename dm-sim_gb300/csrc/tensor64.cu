@@ -104,6 +104,10 @@ struct T64Tables {
   // base minus the free bits, bits 48..55 the bra row exponent ew[1][b] +
   // 128, bit 63 set when its run is stored
   uint64_t outoff[D][D];
+  // the offsets split by their disjoint bit fields: output (a, b) at
+  // offk[a] + offb[b]; allstored: every run of the tile is stored
+  uint64_t offk[D], offb[D];
+  int allstored;
   T64Group<K> grp[2];
   int pk[D], pb[D];  // piece_off of the ket / bra index bits
   int ew[2][D];
@@ -179,8 +183,8 @@ __device__ __forceinline__ void digits_fp64(uint32_t lo, uint32_t hi, uint32_t e
   const uint32_t d = (ecm - (hi & 0x7FF00000u)) >> 20;
   const uint64_t mant = ((uint64_t)((hi & 0x000FFFFFu) | 0x00100000u) << 32) | lo;
   const uint64_t u = shr_u64(mant << 2, d) + kDigitBias;
-  const uint32_t sgn = hi & 0x80000000u;
-  digits_of(u, __uint_as_float(sgn | 0x3F800000u), __uint_as_float(sgn ^ 0xCB000080u), dg);  // +-1, -+(2^23 + 128)
+  const float sg = __uint_as_float((hi & 0x80000000u) | 0x3F800000u);  // +-1 (one integer op)
+  digits_of(u, sg, sg * -8388736.0f, dg);                             // -+(2^23 + 128) on the FP32 pipe
 }
 
 // Digits of a signed integer |v| < 2^55.
@@ -321,6 +325,21 @@ __global__ void __launch_bounds__(kT64Threads, 1)
     off += (uint64_t)(e & ((1 << L) - 1));
     const uint64_t stored = (h.stmask[run >> 5] >> (run & 31)) & 1;
     tb.outoff[bb][a] = off | ((uint64_t)(dp->ew[1][bb] + 128) << 48) | (stored << 63);
+  }
+  if (tid < 2 * D) {
+    const int i = tid & (D - 1), side = tid / D;  // side 0: ket index i, 1: bra index i
+    int e = 0;
+    for (int k = 0; k < K; k++) e |= ((i >> k) & 1) << (side ? h.lbra[k] : h.lket[k]);
+    const int run = e >> L;
+    uint64_t off = 0;
+    for (int j = 0; j < mhi; j++) off |= (uint64_t)((run >> j) & 1) << h.hipos[j];
+    off += (uint64_t)(e & ((1 << L) - 1));
+    (side ? tb.offb : tb.offk)[i] = off;
+  }
+  if (tid == 0) {
+    int all = 1;
+    for (int run = 0; run < (1 << mhi); run++) all &= (int)((h.stmask[run >> 5] >> (run & 31)) & 1);
+    tb.allstored = all;
   }
   if (tid < 8) tb.hipos[tid] = h.hipos[tid];
   if (tid < 256) tb.grp[tid >> 7].brmax[tid & 127] = 0;
@@ -528,6 +547,7 @@ __global__ void __launch_bounds__(kT64Threads, 1)
       tc::fence_after_sync();
       const int pa = (int)mkey_out + tb.ew[0][r] - 1106 - 128;
       uint64_t* arr = (half ? im : re) + tbase + lf;
+      uint64_t* col = arr + tb.offk[r];
 #pragma unroll
       for (int c4 = 0; c4 < D; c4 += 4) {
         float sv[kTc64Orders][4];
@@ -535,13 +555,23 @@ __global__ void __launch_bounds__(kT64Threads, 1)
 #pragma unroll
         for (int o = 0; o < kTc64Orders; o++) tc::tmem_ld4(ta + o * R, sv[o]);
         tc::tmem_wait_ld();
+        if (tb.allstored) {  // the common case: one base per thread, one offset per output
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-          const uint64_t T = tb.outoff[c4 + c][r];
-          if (!(T >> 63)) continue;  // a run the pass does not change
-          const int64_t Y =
-              combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c], sv[6][c], sv[7][c]);
-          arr[T & 0xFFFFFFFFFFFFull] = to_fp64(Y, pa + (int)((T >> 48) & 0xFF));
+          for (int c = 0; c < 4; c++) {
+            const int b = c4 + c;
+            const int64_t Y =
+                combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c], sv[6][c], sv[7][c]);
+            col[tb.offb[b]] = to_fp64(Y, pa + 128 + tb.ew[1][b]);
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < 4; c++) {
+            const uint64_t T = tb.outoff[c4 + c][r];
+            if (!(T >> 63)) continue;  // a run the pass does not change
+            const int64_t Y =
+                combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c], sv[6][c], sv[7][c]);
+            arr[T & 0xFFFFFFFFFFFFull] = to_fp64(Y, pa + (int)((T >> 48) & 0xFF));
+          }
         }
       }
     }
