@@ -95,6 +95,25 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return false;
 }
 
+// ---- named barriers of a thread group (ids >= 1; id 0 is __syncthreads)
+// Barrier `id` over NT threads, and the same with an OR of p over them (every
+// thread of the group gets the same result).
+template <int NT>
+__device__ __forceinline__ void named_bar(int id) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(NT) : "memory");
+}
+template <int NT>
+__device__ __forceinline__ bool named_bar_or(int id, bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred ip, op;\n\tsetp.ne.u32 ip, %1, 0;\n\tbar.red.or.pred op, %2, %3, ip;\n\t"
+      "selp.u32 %0, 1, 0, op;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)p), "r"(id), "n"(NT)
+      : "memory");
+  return r != 0;
+}
+
 // ---- MMA: D[tmem] (+)= A[smem] * B[smem]^T, one thread issues
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
                                          uint32_t accumulate) {

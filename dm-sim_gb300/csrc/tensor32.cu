@@ -100,19 +100,8 @@ constexpr size_t t32_smem_bytes() {
 }
 
 // Named barrier of group g (ids 1, 2), and the same with an OR of p over the group.
-__device__ __forceinline__ void group_bar32(int g) {
-  asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "n"(kT32GroupThreads) : "memory");
-}
-__device__ __forceinline__ bool group_bar_or32(int g, bool p) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred ip, op;\n\tsetp.ne.u32 ip, %1, 0;\n\tbar.red.or.pred op, %2, %3, ip;\n\t"
-      "selp.u32 %0, 1, 0, op;\n\t}"
-      : "=r"(r)
-      : "r"((uint32_t)p), "r"(1 + g), "n"(kT32GroupThreads)
-      : "memory");
-  return r != 0;
-}
+__device__ __forceinline__ void group_bar32(int g) { tc::named_bar<kT32GroupThreads>(1 + g); }
+__device__ __forceinline__ bool group_bar_or32(int g, bool p) { return tc::named_bar_or<kT32GroupThreads>(1 + g, p); }
 
 __device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 v) { return *reinterpret_cast<const uint32_t*>(&v); }
 

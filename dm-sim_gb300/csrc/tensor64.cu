@@ -123,19 +123,8 @@ constexpr size_t t64_smem_bytes() {
 }
 
 // Named barrier of group g (ids 1, 2), and the same with an OR of p over the group.
-__device__ __forceinline__ void group_bar(int g) {
-  asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "n"(kT64GroupThreads) : "memory");
-}
-__device__ __forceinline__ bool group_bar_or(int g, bool p) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred ip, op;\n\tsetp.ne.u32 ip, %1, 0;\n\tbar.red.or.pred op, %2, %3, ip;\n\t"
-      "selp.u32 %0, 1, 0, op;\n\t}"
-      : "=r"(r)
-      : "r"((uint32_t)p), "r"(1 + g), "n"(kT64GroupThreads)
-      : "memory");
-  return r != 0;
-}
+__device__ __forceinline__ void group_bar(int g) { tc::named_bar<kT64GroupThreads>(1 + g); }
+__device__ __forceinline__ bool group_bar_or(int g, bool p) { return tc::named_bar_or<kT64GroupThreads>(1 + g, p); }
 
 __device__ __forceinline__ uint64_t shr_u64(uint64_t x, uint32_t s) {  // s >= 64 gives 0
   uint64_t r;

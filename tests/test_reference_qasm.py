@@ -1,8 +1,9 @@
-"""The OpenQASM 2 frontend on the reference's own circuits (benchmark/*.qasm
-and tool/vqe_uccsd_n8.qasm of pnnl/DM-Sim), where the reference checkout is
+"""The OpenQASM 2 frontend on the reference's own circuits (benchmark/*.qasm,
+tool/vqe_uccsd_n8.qasm and the QASMBench suite it ships under qasmbench/,
+small, medium and large, 55 programs), where the reference checkout is
 present (CPU; skipped elsewhere -- the circuits are not copied into this
-repository): every circuit parses -- the two with classically controlled
-statements under the reference translator's rule of dropping them
+repository): every circuit parses -- those with classically controlled
+statements or resets under the reference translator's rule of dropping them
 (tool/dmsim_qasm.py:104, :321-322) -- and for circuits of up to 10 qubits the
 density-matrix oracle on the parsed circuit equals psi psi^+ of the
 statevector oracle."""
@@ -29,11 +30,11 @@ def reference_dir():
 
 REF = reference_dir()
 FILES = sorted(glob.glob(os.path.join(REF, "benchmark", "*.qasm"))) + [os.path.join(REF, "tool", "vqe_uccsd_n8.qasm")] \
-    if REF else []
+    + sorted(glob.glob(os.path.join(REF, "qasmbench", "*", "*", "*.qasm"))) if REF else []
 
 
 @pytest.mark.skipif(not REF, reason="the reference checkout is not present")
-@pytest.mark.parametrize("path", FILES, ids=[os.path.basename(f) for f in FILES])
+@pytest.mark.parametrize("path", FILES, ids=[os.path.relpath(f, REF) for f in FILES])
 def test_reference_circuit_parses_and_oracles_agree(oracle, path):
     with open(path) as f:
         text = f.read()
