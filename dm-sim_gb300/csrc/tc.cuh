@@ -86,12 +86,25 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: false if the phase did not complete within `limit` polls.
+// try_wait with a suspend-time hint: the thread may be suspended in hardware
+// until the phase completes or `ns` nanoseconds pass, instead of re-polling
+// (a waiting warp then takes no issue slots from the warps that work).
+__device__ __forceinline__ bool mbar_try_wait_hint(uint64_t* bar, uint32_t parity, uint32_t ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: false if the phase did not complete within `limit` polls of
+// at most 128 ns each.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit) {
-  for (uint32_t i = 0; i < limit; i++) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if (i > 64) __nanosleep(64);
-  }
+  for (uint32_t i = 0; i < limit; i++)
+    if (mbar_try_wait_hint(bar, parity, 128)) return true;
   return false;
 }
 

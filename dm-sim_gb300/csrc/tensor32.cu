@@ -15,7 +15,7 @@
 // the FP32-pipe passes' own level.
 //
 // Threads, tiles and synchronisation follow tensor64.cu: 512 threads, two
-// blocks per SM (64 registers a thread, 107 KB of shared memory and 256 TMEM
+// blocks per SM (64 registers a thread, 107 KB of shared memory and 64 TMEM
 // columns a block), two independent groups of 8 warps taking alternate tiles,
 // each with its own tile buffer (1-D TMA bulk copies of the tile's runs, issued
 // one tile ahead), slice operand, accumulator (R TMEM columns), mbarriers and
