@@ -30,21 +30,23 @@
 // warps that take alternate tiles of the block, each with its own tile
 // buffer, digit operand, tensor-memory accumulator set, mbarriers and named
 // barrier: while one group waits at a barrier or on its products, the other
-// issues.  Thread (warp w, lane l) of a group owns tile column m = 32 (w & 3)
-// + l -- the TMEM lane its warp may read -- and half (w >> 2) & 1 of it: the
-// D real or the D imaginary parts.  The group's first thread issues its MMAs;
-// every thread issues its share of the group's bulk copies.  Per tile:
+// issues.  In the digit steps thread (warp w, lane l) of a group owns tile
+// column 16 (w & 7) + (l & 15) and half l >> 4 of it (both halves of a column
+// in one warp); in the accumulator steps column m = 32 (w & 3) + l -- the
+// TMEM lane its warp may read -- and half (w >> 2) & 1: the D real or the D
+// imaginary parts.  The group's first thread issues its MMAs; every thread
+// issues its share of the group's bulk copies.  Per tile:
 //   1. wait for the tile (TMA bulk copies of its runs, issued one tile
-//      ahead), column maxima;  2. ket digits -> A;  3. the ket MMAs
-//   4. ket accumulators -> exact int64 outputs in place of the tile, bra
-//      magnitude keys;  5. bra digits -> A;  6. the bra MMAs, and the group's
-//      next tile loaded into the freed buffer;  7. bra accumulators -> FP64
+//      ahead), column maxima, ket digits -> A;  2. the ket MMAs;
+//   3. ket accumulators -> exact int64 outputs in place of the tile, bra
+//      magnitude keys;  4. bra digits -> A;  5. the bra MMAs, and the group's
+//      next tile loaded into the freed buffer;  6. bra accumulators -> FP64
 //      -> global stores.
-// Four group barriers per tile (after steps 1, 2, 4 and 5); the ones after
-// steps 1 and 4 also OR the threads' timeout flags.  Every wait is bounded; on
-// expiry the group leaves its loop at the next such barrier, waits (bounded)
-// for its own copies and MMAs in flight, sets the error flag, and the block
-// releases its TMEM; the host reports DMSIM_ERR_TIMEOUT.
+// Three group barriers per tile (after steps 1, 3 and 4); the first two also
+// OR the threads' timeout flags.  Every wait is bounded; on expiry the group
+// leaves its loop at the next such barrier, waits (bounded) for its own copies
+// and MMAs in flight, sets the error flag, and the block releases its TMEM;
+// the host reports DMSIM_ERR_TIMEOUT.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
