@@ -41,7 +41,7 @@ int tc_blocks_per_sm(int K, int arith);
 // persistent 512-thread blocks per SM.
 cudaError_t launch_pass_tc32(const LaunchArgs& a, cudaStream_t s);
 // FP64-width tensor-core passes on an FP64 state (tensor64.cu): one
-// persistent 512-thread block per SM.
+// persistent 1024-thread block per SM.
 cudaError_t launch_pass_tc64(const LaunchArgs& a, cudaStream_t s);
 // In place: FP64 entries <-> double-float pairs (the fused path's working format)
 cudaError_t launch_to_df64(void* re, void* im, uint64_t N, unsigned grid, cudaStream_t s);

@@ -26,16 +26,18 @@
 // entries): the error of an output is below 2^-54 of its operator row's
 // 1-norm times its column's largest value, per step.
 //
-// Threads: 512 (16 warps), one block per SM, as two independent groups of 8
-// warps that take alternate tiles of the block, each with its own tile
-// buffer, digit operand, tensor-memory accumulator set, mbarriers and named
-// barrier: while one group waits at a barrier or on its products, the other
-// issues.  In the digit steps thread (warp w, lane l) of a group owns tile
-// column 16 (w & 7) + (l & 15) and half l >> 4 of it (both halves of a column
-// in one warp); in the accumulator steps column m = 32 (w & 3) + l -- the
-// TMEM lane its warp may read -- and half (w >> 2) & 1: the D real or the D
-// imaginary parts.  The group's first thread issues its MMAs; every thread
-// issues its share of the group's bulk copies.  Per tile:
+// Threads: 1024 (32 warps, 64 registers each), one block per SM, as two
+// independent groups of 16 warps that take alternate tiles of the block, each
+// with its own tile buffer, digit operand, tensor-memory accumulator set,
+// mbarriers and named barrier: while one group waits at a barrier or on its
+// products, the other issues, with eight warps per scheduler to hide the
+// integer work's latency.  Every thread holds a quarter of a column: in the
+// digit steps thread (warp w, lane l) of a group owns tile column 8 (w & 15)
+// + (l & 7) and quarter l >> 3 of it (half l >> 4, values (l >> 3) & 1 of
+// that half; the four quarters of a column in one warp); in the accumulator
+// steps column m = 32 (w & 3) + l -- the TMEM lane quadrant its warp may read
+// -- and quarter ((w & 15) >> 2).  The group's first thread issues its MMAs;
+// every thread issues its share of the group's bulk copies.  Per tile:
 //   1. wait for the tile (TMA bulk copies of its runs, issued one tile
 //      ahead), column maxima, ket digits -> A;  2. the ket MMAs;
 //   3. ket accumulators -> exact int64 outputs in place of the tile, bra
@@ -59,8 +61,8 @@ namespace dmg {
 
 namespace {
 
-constexpr int kT64Threads = 512;
-constexpr int kT64GroupThreads = 256;
+constexpr int kT64Threads = 1024;
+constexpr int kT64GroupThreads = 512;
 constexpr uint32_t kT64WaitPolls = 1u << 24;
 
 template <int K>
@@ -151,36 +153,60 @@ __device__ __forceinline__ float byte_float(uint32_t x, uint32_t sel) {
   return __uint_as_float(__byte_perm(x, kMagicHi, sel));
 }
 
-// The 7 digits (digit 0 the most significant) of the balanced base-256
-// representation of u - B, B = 0x80 in bytes 0..6, each times s and shifted
-// by c: digit j = (byte_{6-j}(u) - 128) s, the top one from bits 48..56.
-__device__ __forceinline__ void digits_of(uint64_t u, float s, float c, float (&dg)[kTc64Slices]) {
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);  // exact: |digit| <= 128
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// Digit j (0 the most significant) of the balanced base-256 representation
+// of u - B, B = 0x80 in bytes 0..6, times s (+-1): (byte_{6-j}(u) - 128) s,
+// the top one from bits 48..56; float (2^23 + byte) from a byte permute, then
+// one FMA with c = -(2^23 + 128) s.
+__device__ __forceinline__ float digit_of(uint64_t u, int j, float s, float c) {
   const uint32_t ul = (uint32_t)u, uh = (uint32_t)(u >> 32);
-  dg[6] = fmaf(byte_float(ul, 0x7540), s, c);
-  dg[5] = fmaf(byte_float(ul, 0x7541), s, c);
-  dg[4] = fmaf(byte_float(ul, 0x7542), s, c);
-  dg[3] = fmaf(byte_float(ul, 0x7543), s, c);
-  dg[2] = fmaf(byte_float(uh, 0x7540), s, c);
-  dg[1] = fmaf(byte_float(uh, 0x7541), s, c);
-  dg[0] = fmaf(byte_float(uh, 0x7532), s, c);
+  switch (j) {
+    case 0: return fmaf(byte_float(uh, 0x7532), s, c);
+    case 1: return fmaf(byte_float(uh, 0x7541), s, c);
+    case 2: return fmaf(byte_float(uh, 0x7540), s, c);
+    case 3: return fmaf(byte_float(ul, 0x7543), s, c);
+    case 4: return fmaf(byte_float(ul, 0x7542), s, c);
+    case 5: return fmaf(byte_float(ul, 0x7541), s, c);
+    default: return fmaf(byte_float(ul, 0x7540), s, c);
+  }
 }
 constexpr uint64_t kDigitBias = 0x0080808080808080ull;
 
-// Digits of an FP64 value (bits lo, hi) on its column's grid: ecm is the
-// column's largest exponent field (hi & 0x7FF00000, at least 64 << 20).
-// v = |x| 2^(1077 - Ec) = (mantissa << 2) >> (Ec - E) < 2^55; the sign is
-// applied to every digit.  Zeros and subnormals (exponent field 0) shift out.
-__device__ __forceinline__ void digits_fp64(uint32_t lo, uint32_t hi, uint32_t ecm, float (&dg)[kTc64Slices]) {
+// An FP64 value (bits lo, hi) on its column's grid, as u = v + B and its sign
+// s = +-1: ecm is the column's largest exponent field (hi & 0x7FF00000, at
+// least 64 << 20); v = |x| 2^(1077 - Ec) = (mantissa << 2) >> (Ec - E) <
+// 2^55.  Zeros and subnormals (exponent field 0) shift out.
+__device__ __forceinline__ uint64_t align_fp64(uint32_t lo, uint32_t hi, uint32_t ecm, float& s) {
   const uint32_t d = (ecm - (hi & 0x7FF00000u)) >> 20;
   const uint64_t mant = ((uint64_t)((hi & 0x000FFFFFu) | 0x00100000u) << 32) | lo;
-  const uint64_t u = shr_u64(mant << 2, d) + kDigitBias;
-  const float sg = __uint_as_float((hi & 0x80000000u) | 0x3F800000u);  // +-1 (one integer op)
-  digits_of(u, sg, sg * -8388736.0f, dg);                             // -+(2^23 + 128) on the FP32 pipe
+  s = __uint_as_float((hi & 0x80000000u) | 0x3F800000u);  // +-1 (one integer op)
+  return shr_u64(mant << 2, d) + kDigitBias;
 }
 
-// Digits of a signed integer |v| < 2^55.
-__device__ __forceinline__ void digits_int(int64_t v, float (&dg)[kTc64Slices]) {
-  digits_of((uint64_t)v + kDigitBias, 1.0f, -8388736.0f, dg);  // -(2^23 + 128)
+// Store the 7 digit slices of NV consecutive K indices (k0 ..) of operand row
+// `row`: per slice, the digits of value pairs packed in BF16 pairs, one
+// 16-byte (NV = 8) or 8-byte (NV = 4) store.  u: values + B, s: their signs.
+template <int NV>
+__device__ __forceinline__ void store_digits(unsigned char* sA, uint32_t a_bytes, uint32_t off,
+                                             const uint64_t (&u)[NV], const float (&s)[NV]) {
+#pragma unroll
+  for (int j = 0; j < kTc64Slices; j++) {
+    uint32_t pk[NV / 2];
+#pragma unroll
+    for (int p = 0; p < NV / 2; p++) {
+      const float d0 = digit_of(u[2 * p], j, s[2 * p], s[2 * p] * -8388736.0f);
+      const float d1 = digit_of(u[2 * p + 1], j, s[2 * p + 1], s[2 * p + 1] * -8388736.0f);
+      pk[p] = pack_bf16x2(d0, d1);
+    }
+    if constexpr (NV == 8)
+      *reinterpret_cast<uint4*>(sA + j * a_bytes + off) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    else
+      *reinterpret_cast<uint2*>(sA + j * a_bytes + off) = make_uint2(pk[0], pk[1]);
+  }
 }
 
 // Y = sum_o S_o 2^(8(5-o)) for o <= 5, plus floor((S_6 2^8 + S_7) / 2^16),
@@ -209,25 +235,6 @@ __device__ __forceinline__ uint64_t to_fp64(int64_t Y, int P) {
   return (Y != 0 && E > 0) ? b + ((uint64_t)(int64_t)P << 52) : 0ull;
 }
 
-__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
-  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);  // exact: |digit| <= 128
-  return *reinterpret_cast<const uint32_t*>(&v);
-}
-
-// Store the packed digits of Q consecutive K indices of row m (pk[i][j]:
-// values 2i, 2i+1 of slice j) into the K-major operand, one 16-byte (Q = 8)
-// or 8-byte (Q = 4) store per slice.
-template <int Q>
-__device__ __forceinline__ void store_packed(unsigned char* sA, uint32_t a_bytes, uint32_t off,
-                                             const uint32_t (&pk)[Q / 2][kTc64Slices]) {
-#pragma unroll
-  for (int j = 0; j < kTc64Slices; j++) {
-    if constexpr (Q == 8)
-      *reinterpret_cast<uint4*>(sA + j * a_bytes + off) = make_uint4(pk[0][j], pk[1][j], pk[2][j], pk[3][j]);
-    else
-      *reinterpret_cast<uint2*>(sA + j * a_bytes + off) = make_uint2(pk[0][j], pk[1][j]);
-  }
-}
 
 // One thread issues every product of a step: digit slices A_0..A_6 of the
 // 128 columns against the operator's slices, slice pairs of orders 0..7, the
@@ -268,14 +275,17 @@ __global__ void __launch_bounds__(kT64Threads, 1)
   T64Tables<K>& tb = *reinterpret_cast<T64Tables<K>*>(bufs + 4 * ASTR);
   const PassHeader& h = dp->h;
   const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
-  const int g = w >> 3, gtid = tid & (kT64GroupThreads - 1);
-  // digit steps: column mc = 16 (w & 7) + (l & 15), half hc = l >> 4 (both
-  // halves of a column in one warp)
-  const int mc = 16 * (w & 7) + (l & 15), hc = l >> 4;
+  const int g = w >> 4, gtid = tid & (kT64GroupThreads - 1), wg = w & 15;
+  constexpr int NV = D / 2;  // values a thread holds: a quarter of a column's 2D reals
+  // digit steps: column mc = 8 wg + (l & 7), quarter qc = l >> 3 -- half hc =
+  // qc >> 1 (real or imaginary parts), values cc NV .. cc NV + NV - 1 of it,
+  // cc = qc & 1 (the four quarters of a column in one warp)
+  const int mc = 8 * wg + (l & 7), qc = l >> 3, hc = qc >> 1, cc = qc & 1;
   const int rc = mc / G, fc = mc & (G - 1);
-  // accumulator steps: column m = 32 (w & 3) + l -- the TMEM lane its warp
-  // may read -- half (w >> 2) & 1
-  const int m = 32 * (w & 3) + l, half = (w >> 2) & 1;
+  // accumulator steps: column m = 32 (w & 3) + l -- the TMEM lane quadrant
+  // its warp may read -- quarter q = (wg >> 2) & 3: half q >> 1, values
+  // chunk NV .. of it, chunk = q & 1
+  const int m = 32 * (w & 3) + l, q = (wg >> 2) & 3, half = q >> 1, chunk = q & 1;
   const int r = m / G, f = m & (G - 1);
   unsigned char* sA = smem + g * kTc64Slices * S::A_BYTES;  // the group's digit operand (ket, then bra)
   uint64_t* buf = bufs + (size_t)g * 2 * ASTR;             // the group's tile, then its ket outputs
@@ -358,13 +368,10 @@ __global__ void __launch_bounds__(kT64Threads, 1)
     return o;
   };
   const int lf = free_off(f);  // accumulator steps: free offset of column (., f) in the state
-  // digit steps: column (b = rc, fc)'s values a = 0..D-1 of half hc at buf[posk[a]]
-  int posk[D];
-  {
-    const int basec = hc * ASTR + tb.pb[rc] + piece_off(free_off(fc));
-#pragma unroll
-    for (int a = 0; a < D; a++) posk[a] = basec + tb.pk[a];
-  }
+  // digit steps: column (b = rc, fc)'s values a = cc NV + i of half hc at
+  // buf[basec + tb.pk[cc NV + i]] (the offsets read from shared memory, a
+  // broadcast per 8 lanes, to keep the 64-register budget)
+  const int basec = hc * ASTR + tb.pb[rc] + piece_off(free_off(fc));
   const uint64_t ntiles = h.ntiles, gstep = 2 * (uint64_t)gridDim.x;
   const int runlen = 1 << L, lgp = L < 4 ? L : 4, npieces = (2 * TILE) >> lgp;
   // The ket step's exact integer outputs Y(a, b) of column (b, ff) replace
@@ -421,33 +428,26 @@ __global__ void __launch_bounds__(kT64Threads, 1)
   }
 
   for (; t < ntiles; t += gstep) {
-    // ---- 1: the tile's values of column (b = rc, fc), its grid (the largest
-    // exponent of both halves, one shuffle away), its ket digits
+    // ---- 1: the tile's values of column (b = rc, fc), quarter qc, its grid
+    // (the largest exponent of the column's four quarters, two shuffles
+    // away), its ket digits
     wait(&gp.full, phf, pendf);
     {
-      uint64_t v[D];
+      uint64_t u[NV];
+      float sg[NV];
       uint32_t emx = 0;
 #pragma unroll
-      for (int a = 0; a < D; a++) {
-        v[a] = buf[posk[a]];
-        emx = max(emx, (uint32_t)(v[a] >> 32) & 0x7FF00000u);
+      for (int i = 0; i < NV; i++) {
+        u[i] = buf[basec + tb.pk[cc * NV + i]];
+        emx = max(emx, (uint32_t)(u[i] >> 32) & 0x7FF00000u);
       }
-      const uint32_t ecm = max(max(emx, __shfl_xor_sync(0xffffffffu, emx, 16)), 64u << 20);
-      if (hc == 0) gp.colEt[rc][fc] = (int)(ecm >> 20);
+      emx = max(emx, __shfl_xor_sync(0xffffffffu, emx, 8));
+      emx = max(emx, __shfl_xor_sync(0xffffffffu, emx, 16));
+      const uint32_t ecm = max(emx, 64u << 20);
+      if (qc == 0) gp.colEt[rc][fc] = (int)(ecm >> 20);
 #pragma unroll
-      for (int ch = 0; ch < D / 8; ch++) {
-        uint32_t pk[4][kTc64Slices];
-#pragma unroll
-        for (int c2 = 0; c2 < 4; c2++) {
-          float d0[kTc64Slices], d1[kTc64Slices];
-          const uint64_t v0 = v[8 * ch + 2 * c2], v1 = v[8 * ch + 2 * c2 + 1];
-          digits_fp64((uint32_t)v0, (uint32_t)(v0 >> 32), ecm, d0);
-          digits_fp64((uint32_t)v1, (uint32_t)(v1 >> 32), ecm, d1);
-#pragma unroll
-          for (int j = 0; j < kTc64Slices; j++) pk[c2][j] = pack_bf16x2(d0[j], d1[j]);
-        }
-        store_packed<8>(sA, S::A_BYTES, tc_kmajor_offset(mc, hc * D + 8 * ch, S::SBO), pk);
-      }
+      for (int i = 0; i < NV; i++) u[i] = align_fp64((uint32_t)u[i], (uint32_t)(u[i] >> 32), ecm, sg[i]);
+      store_digits<NV>(sA, S::A_BYTES, tc_kmajor_offset(mc, hc * D + cc * NV, S::SBO), u, sg);
     }
     tc::fence_proxy_async_smem();
     tc::fence_before_sync();
@@ -468,15 +468,15 @@ __global__ void __launch_bounds__(kT64Threads, 1)
       tc::fence_after_sync();
       const uint32_t Ec = (uint32_t)gp.colEt[r][f];
 #pragma unroll
-      for (int c4 = 0; c4 < D; c4 += 4) {
+      for (int c4 = 0; c4 < NV; c4 += 4) {
         float sv[kTc64Orders][4];
-        const uint32_t ta = tmem + tlane + half * D + c4;
+        const uint32_t ta = tmem + tlane + half * D + chunk * NV + c4;
 #pragma unroll
         for (int o = 0; o < kTc64Orders; o++) tc::tmem_ld4(ta + o * R, sv[o]);
         tc::tmem_wait_ld();
 #pragma unroll
         for (int c = 0; c < 4; c++) {
-          const int a = c4 + c;
+          const int a = chunk * NV + c4 + c;
           buf[yoff(half, a, r, f)] = (uint64_t)combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c],
                                                               sv[5][c], sv[6][c], sv[7][c]);
           const float mag = fmaf(fabsf(sv[1][c]), 0.00390625f, fabsf(sv[0][c])) + 65.0f;
@@ -488,30 +488,23 @@ __global__ void __launch_bounds__(kT64Threads, 1)
     if (group_bar_or(g, bad)) break;
     tc::fence_after_sync();
 
-    // ---- 4: bra digits of column (a = rc, fc): values Y_b 2^Ec(b) on the
-    // grid 2^(mkey - 141), |v| < 2^55 (1 + 2^-23)
+    // ---- 4: bra digits of column (a = rc, fc), quarter qc: values Y_b
+    // 2^Ec(b) on the grid 2^(mkey - 141), |v| < 2^55 (1 + 2^-23)
     const uint32_t mkey_out = gp.brmax[m];  // the key of this thread's column in step 6
     {
       const uint32_t mkey = gp.brmax[mc];
+      uint64_t u[NV];
+      float sg[NV];
 #pragma unroll
-      for (int ch = 0; ch < D / 8; ch++) {
-        uint32_t pk[4][kTc64Slices];
-#pragma unroll
-        for (int c2 = 0; c2 < 4; c2++) {
-          float d[2][kTc64Slices];
-#pragma unroll
-          for (int u = 0; u < 2; u++) {
-            const int b = 8 * ch + 2 * c2 + u;
-            const int64_t Y = (int64_t)buf[yoff(hc, rc, b, fc)];
-            const int sh = (int)mkey - 141 - gp.colEt[b][fc];
-            const int64_t v = sh >= 0 ? shr_s64(Y, (uint32_t)sh) : shl_s64(Y, (uint32_t)(-sh));
-            digits_int(v, d[u]);
-          }
-#pragma unroll
-          for (int j = 0; j < kTc64Slices; j++) pk[c2][j] = pack_bf16x2(d[0][j], d[1][j]);
-        }
-        store_packed<8>(sA, S::A_BYTES, tc_kmajor_offset(mc, hc * D + 8 * ch, S::SBO), pk);
+      for (int i = 0; i < NV; i++) {
+        const int b = cc * NV + i;
+        const int64_t Y = (int64_t)buf[yoff(hc, rc, b, fc)];
+        const int sh = (int)mkey - 141 - gp.colEt[b][fc];
+        const int64_t v = sh >= 0 ? shr_s64(Y, (uint32_t)sh) : shl_s64(Y, (uint32_t)(-sh));
+        u[i] = (uint64_t)v + kDigitBias;
+        sg[i] = 1.0f;
       }
+      store_digits<NV>(sA, S::A_BYTES, tc_kmajor_offset(mc, hc * D + cc * NV, S::SBO), u, sg);
     }
     const uint64_t tn = t + gstep;
     if (gtid == 0 && tn < ntiles) tc::mbar_arrive_expect_tx(&gp.full, S::TX_BYTES);  // the group's next tile
@@ -540,16 +533,16 @@ __global__ void __launch_bounds__(kT64Threads, 1)
       uint64_t* arr = (half ? im : re) + tbase + lf;
       uint64_t* col = arr + tb.offk[r];
 #pragma unroll
-      for (int c4 = 0; c4 < D; c4 += 4) {
+      for (int c4 = 0; c4 < NV; c4 += 4) {
         float sv[kTc64Orders][4];
-        const uint32_t ta = tmem + tlane + half * D + c4;
+        const uint32_t ta = tmem + tlane + half * D + chunk * NV + c4;
 #pragma unroll
         for (int o = 0; o < kTc64Orders; o++) tc::tmem_ld4(ta + o * R, sv[o]);
         tc::tmem_wait_ld();
         if (tb.allstored) {  // the common case: one base per thread, one offset per output
 #pragma unroll
           for (int c = 0; c < 4; c++) {
-            const int b = c4 + c;
+            const int b = chunk * NV + c4 + c;
             const int64_t Y =
                 combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c], sv[6][c], sv[7][c]);
             col[tb.offb[b]] = to_fp64(Y, pa + 128 + tb.ew[1][b]);
@@ -557,7 +550,7 @@ __global__ void __launch_bounds__(kT64Threads, 1)
         } else {
 #pragma unroll
           for (int c = 0; c < 4; c++) {
-            const uint64_t T = tb.outoff[c4 + c][r];
+            const uint64_t T = tb.outoff[chunk * NV + c4 + c][r];
             if (!(T >> 63)) continue;  // a run the pass does not change
             const int64_t Y =
                 combine_orders(sv[0][c], sv[1][c], sv[2][c], sv[3][c], sv[4][c], sv[5][c], sv[6][c], sv[7][c]);
