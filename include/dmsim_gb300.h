@@ -48,10 +48,11 @@ enum dmsim_option {
   DMSIM_OPT_RENORM = 10,     /* complex64: FP64 trace + Hermitian renormalisation every R passes and at the end [64]; 0 = off */
   DMSIM_OPT_PLAIN_ARITH = 11, /* plain FP64 runs (FP64 state at rest): 0 = FP64 passes [0] (dense passes bound by
                                  GB300's FP64 pipe), 1 = double-float passes on the FP32 pipe (HBM-bound) */
-  DMSIM_OPT_TENSOR = 12,      /* 3- and 4-qubit dense/sparse passes on the tensor cores (BF16 digits, exact
-                                 FP32 sums): 1 = where the learned planner picks them, else every eligible
-                                 pass of an FP64-width run and, in double-float runs, passes above a density
-                                 rule [1]; 0 = never; 2 = every eligible pass, complex64 runs included */
+  DMSIM_OPT_TENSOR = 12,      /* 3- and 4-qubit dense/sparse passes on the tensor cores (BF16 digits): 1 =
+                                 where the learned planner picks them, else every eligible pass of an
+                                 FP64-width run, the 4-qubit passes of a complex64 run (BF16 x 3 split, FP32
+                                 accumulation) and, in double-float runs, passes above a density rule [1];
+                                 0 = never; 2 = every eligible pass */
   DMSIM_OPT_DIRECT1 = 13      /* 1 = 1-qubit move/sign/phase/dense passes on the register kernel (no shared-memory
                                  tiles) [1], 0 = the tiled kernel */
 };
