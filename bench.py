@@ -102,6 +102,24 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(value, world, device):
+    """The largest of the ranks' values (the slowest replica's step time):
+    an all-reduce MAX over the default process group when world > 1."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_seconds_per_circuit(step_ms, world):
+    """Whole-job aggregate of the replicas: every rank runs one circuit per
+    step, so the job finishes world circuits per (slowest) step time."""
+    return step_ms / 1e3 / world
+
+
 def workload(n, gates):
     return W.table_mix(n, gates, seed=2)
 
@@ -445,12 +463,7 @@ def main():
         ms.append(fused.last_timings()["ms"])
     wall = time.perf_counter() - t_wall0
     clk = clocks.stop()
-    step_ms = float(np.mean(ms))
-    if world > 1:
-        import torch
-        t = torch.tensor([step_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms = float(t.item())
+    step_ms = max_over_ranks(float(np.mean(ms)), world, "cuda")
     bytes_per_run = fused.last_timings()["bytes"]
     launches_per_run = int(fused.last_timings()["passes"])
 
@@ -538,8 +551,7 @@ def main():
         q16 = config16(args, tensor, not args.no_plain, not args.no_cpu)
 
     if rank == 0:
-        # whole-job aggregate: the world's ranks each ran one circuit per step
-        value = step_ms / 1e3 / world
+        value = whole_job_seconds_per_circuit(step_ms, world)
         line = {
             "metric": METRIC,
             "value": value, "unit": "s/circuit", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
