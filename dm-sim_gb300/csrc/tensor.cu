@@ -1,6 +1,8 @@
-// tensor.cu -- dense K = 3, 4 qubit passes on the tensor cores (tcgen05):
-// double-float state with FP64-level accuracy (6 slices), or complex64 (FP32)
-// state with FP32-level accuracy (3 slices).
+// tensor.cu -- dense K = 3, 4 qubit passes on the tensor cores (tcgen05) for
+// a double-float state, with FP64-level accuracy (6 slices).  The kernel is
+// written for an FP32 element type as well (3 slices), but complex64 states
+// run the per-value BF16 x 3 kernel of tensor32.cu, so only the double-float
+// instance is built.
 //
 // A tile is 128 columns of one step: in the ket step column m = (b, f) holds
 // the 2^K entries rho[(., b, f)], in the bra step column m = (a, f) holds
@@ -468,8 +470,7 @@ static cudaError_t launch_tc_k(const LaunchArgs& a, cudaStream_t s) {
 cudaError_t launch_pass_tc(const LaunchArgs& a, cudaStream_t s) {
   if (!a.err || (a.K != 3 && a.K != 4)) return cudaErrorInvalidValue;
   if (a.arith == AR_DF64) return a.K == 3 ? launch_tc_k<3, df64>(a, s) : launch_tc_k<4, df64>(a, s);
-  if (a.arith == AR_FP32) return a.K == 3 ? launch_tc_k<3, float>(a, s) : launch_tc_k<4, float>(a, s);
-  return cudaErrorInvalidValue;
+  return cudaErrorInvalidValue;  // FP64 states: tensor64.cu; complex64 states: tensor32.cu
 }
 
 // Resident blocks per SM from the kernel's own resources: shared memory
